@@ -1,0 +1,381 @@
+"""Benchmark of the MCRG Monte-Carlo / block-spin hot path on GB300.
+
+Default workload ("large"): one L = 16384 periodic 2D Ising lattice
+(268M int8 spins, HBM-resident), K = -0.4406868, 13 RG levels (b = 2
+majority rule), 5 couplings.  One step = `--sweeps-per-step` fused
+checkerboard sweeps + one full measurement (blocking of every level,
+coupling sums, exact int128 moment products).  Metric: Gflips/s =
+L^2 * sweeps / s (site updates).  The lattice (268 MB) is larger than L2
+(129 MB), so no L2 flush is needed between steps.
+
+Other workloads (--workload): "batched" (4096 replicas, L from
+{16..256}, one launch per side, CUDA graph), "plain" (one L = 64 lattice,
+one CTA per launch), "served" (Poisson arrivals into mcrg_server).
+
+--impl reference times the reference's CPU path (its Wolff update +
+calc_interactions + block_spin_transformation sample loop, restated in
+oracle/) on the host cores for the same workload.
+
+Multi-GPU: replicas only (each rank runs its own chain, replica = rank);
+value = all ranks' flips / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+KC = -math.log(1.0 + math.sqrt(2.0)) / 2.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """Per-launch DRAM bytes of a kernel from a committed ncu summary line
+    'traffic_bytes_per_launch <kernel> <workload> <bytes>' in profiles/*.txt."""
+    d = os.path.join(ROOT, "profiles")
+    try:
+        for fn in sorted(os.listdir(d)):
+            if not fn.endswith(".txt"):
+                continue
+            for ln in open(os.path.join(d, fn)):
+                f = ln.split()
+                if len(f) == 4 and f[0] == "traffic_bytes_per_launch" and f[1] == name:
+                    return int(float(f[3]))
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def run_large(args, D: Dist) -> dict:
+    import torch
+    import mcrg_gb300 as M
+    from mcrg_gb300 import _abi
+
+    dev = D.local
+    torch.cuda.set_device(dev)
+    L, spp, C_ = args.L, args.sweeps_per_step, args.couplings
+    lat = M.Lattice(L, KC, seed=1, replica=D.rank, n_couplings=C_, device=dev)
+    stream = torch.cuda.ExternalStream(lat.stream(), device=dev)
+    flips_per_step = float(L) * L * spp
+
+    # warm-up (also runs the chain out of the random start)
+    lat.measure(args.warmup, spp)
+    lat.sync()
+
+    # ---- device-resident throughput over exactly K steps
+    clk = Clocks(dev)
+    clk.start()
+    D.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    tot, _ = lat.measure(args.steps, spp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    D.barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    ms_max = D.max(ms)
+    value = D.world * flips_per_step * args.steps / (ms_max * 1e-3) / 1e9
+
+    # ---- dominant kernel alone: the fused sweep, per launch
+    n_sw = max(8, spp)
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    lat.sweep(n_sw)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    sweep_ms = s0.elapsed_time(s1) / n_sw
+    alg_bytes = 2.0 * L * L  # one read + one write of every int8 site
+    peak, kind = peaks()
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    traffic = profiled_traffic("tiled_sweep_kernel")
+
+    # ---- end to end through the C ABI with host buffers
+    hspins = torch.empty((L, L), dtype=torch.int8, pin_memory=True)
+    hspins.copy_(torch.from_numpy(lat.spins_))
+    hptr = C.c_void_p(hspins.data_ptr())
+    mom = _abi.Moments()
+    lib = M.lib()
+    for _ in range(2):
+        _abi.check(lib.mcrg_set_spins(lat._ctx, hptr), "mcrg_set_spins")
+        _abi.check(lib.mcrg_measure(lat._ctx, 1, spp, C.byref(mom), 0, None, 0), "mcrg_measure")
+    D.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _abi.check(lib.mcrg_set_spins(lat._ctx, hptr), "mcrg_set_spins")
+        _abi.check(lib.mcrg_measure(lat._ctx, 1, spp, C.byref(mom), 0, None, 0), "mcrg_measure")
+    e2e_s = D.max(time.perf_counter() - t0)
+    e2e = D.world * flips_per_step * args.steps / e2e_s / 1e9
+    lat.close()
+
+    n_hbm_levels = sum(1 for l in range(0, 14) if (L >> l) > 256 and l <= int(math.log2(L)) - 1)
+    launches = args.steps * (spp + n_hbm_levels + 1)
+    return {
+        "metric": "Gflips/s", "value": round(value, 2), "unit": "Gflips/s", "n_gpus": D.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (Philox-seeded initial spins; no dataset involved)",
+        "config": {"workload": "large: L=16384 periodic 2D Ising, K=-0.4406868, 13 RG levels b=2, "
+                               "%d couplings, %d sweeps + 1 measurement per step" % (C_, spp),
+                   "L": L, "K": KC, "levels": int(math.log2(L)) - 1, "couplings": C_, "sweeps_per_step": spp,
+                   "parallelism": "replicas x%d" % D.world, "l2": "inputs larger than L2 (268 MB lattice)"},
+        "e2e": {"value": round(e2e, 2), "unit": "Gflips/s", "h2d_bytes_per_step": L * L,
+                "d2h_bytes_per_step": C.sizeof(_abi.Moments)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": "tiled_sweep_kernel", "peak_kind": kind,
+                     "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(sweep_ms, 4)},
+        "clocks": clocks,
+        "moments_samples": tot.n_samples,
+    }
+
+
+def run_batched(args, D: Dist) -> dict:
+    """4096 replicas, L ~ {16:.3, 32:.3, 64:.2, 128:.15, 256:.05}, K on a 33-point grid."""
+    import numpy as np
+    import torch
+    import mcrg_gb300 as M
+
+    torch.cuda.set_device(D.local)
+    rng = np.random.default_rng(7 + D.rank)
+    Ls = rng.choice([16, 32, 64, 128, 256], size=args.replicas, p=[0.3, 0.3, 0.2, 0.15, 0.05])
+    Ks = np.linspace(-0.49, -0.43, 33)
+    reqs = [M.make_request(int(L), float(Ks[i % 33]), seed=1 + i, replica=D.rank * args.replicas + i,
+                           n_eq=0, n_samples=args.batch_sweeps, sweeps_between=1, n_couplings=2)
+            for i, L in enumerate(Ls)]
+    flips = float(sum(int(L) * int(L) for L in Ls)) * args.batch_sweeps
+    for _ in range(args.warmup):
+        M.batch_run(reqs, device=D.local)
+    D.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        M.batch_run(reqs, device=D.local)
+    torch.cuda.synchronize()
+    dt = D.max(time.perf_counter() - t0)
+    value = D.world * flips * args.steps / dt / 1e9
+    return {"metric": "Gflips/s", "value": round(value, 2), "unit": "Gflips/s", "n_gpus": D.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic", "solves_per_s": round(D.world * len(reqs) * args.steps / dt, 1),
+            "config": {"workload": "batched: %d replicas, L in {16..256}, K grid [-0.49,-0.43], %d sweeps each "
+                                   "(measured every sweep)" % (args.replicas, args.batch_sweeps),
+                       "parallelism": "replicas x%d" % D.world}}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference's CPU path (restated), all host threads
+# ---------------------------------------------------------------------------
+def cpu_reference(L: int, seconds: float, threads: int, n_couplings: int = 2) -> dict:
+    """The reference's sample loop (src/mcrg.cpp:72-98: one Wolff update, then
+    coupling sums + blocking at every level) on `threads` independent replicas,
+    each on its own OS thread, for about `seconds`."""
+    from oracle import oracle as O
+    nl = int(math.log2(L)) - 1
+    res = [None] * threads
+
+    def work(k):
+        s = O.init_spins(L, 1000 + k)
+        s[:] = 1  # ordered start: Wolff relaxes from it in a few steps at K = Kc
+        w = O.Wolff(L, KC, 1000 + k)
+        w.steps(s, 3)
+        t0 = time.perf_counter()
+        flipped = samples = 0
+        while True:
+            flipped += w.steps(s, 1)
+            O.measure(s, n_couplings, nl, 1000 + k, 0, samples)
+            samples += 1
+            if time.perf_counter() - t0 > seconds:
+                break
+        w.close()
+        res[k] = (flipped, samples, time.perf_counter() - t0)
+
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    flipped = sum(r[0] for r in res)
+    samples = sum(r[1] for r in res)
+    return {"flips_per_s": flipped / wall, "samples": samples, "wall_s": wall}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="large", choices=["large", "batched"])
+    ap.add_argument("--L", type=int, default=16384)
+    ap.add_argument("--sweeps-per-step", type=int, default=10)
+    ap.add_argument("--couplings", type=int, default=5)
+    ap.add_argument("--replicas", type=int, default=4096)
+    ap.add_argument("--batch-sweeps", type=int, default=1000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    D = Dist()
+
+    if args.impl == "reference":
+        if D.rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        per = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+        vals = []
+        for _ in range(args.warmup):
+            cpu_reference(args.L, per / 2, threads)
+        for _ in range(args.steps):
+            vals.append(cpu_reference(args.L, per, threads))
+        fl = sum(v["flips_per_s"] for v in vals) / len(vals) / 1e9
+        out = {"impl": "reference", "metric": "Gflips/s", "value": round(fl, 4), "unit": "Gflips/s",
+               "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "i8", "data": "synthetic",
+               "config": {"workload": "large: L=%d periodic 2D Ising, K=-0.4406868 (reference Wolff update + "
+                                      "all-level measurement per sample)" % args.L},
+               "cpu_baseline": {"value": round(fl, 4), "unit": "Gflips/s", "cores": threads, "kind": "port",
+                                "sample": "%d threads x ~%.1f s of Wolff steps + measurement on L=%d replicas"
+                                          % (threads, per, args.L)},
+               "e2e": {"value": round(fl, 4), "unit": "Gflips/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
+        return
+
+    if args.workload == "large":
+        out = run_large(args, D)
+    else:
+        out = run_batched(args, D)
+    if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": round(cb["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "reference Wolff update + measurement, %d independent replicas on %d "
+                                         "threads for %.1f s (%d samples)" % (threads, threads, cb["wall_s"],
+                                                                             cb["samples"])}
+    if D.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * mcrg.h -- C ABI of the GB300-native MCRG hot path (libmcrg.so).
+ *
+ * Drop-in boundary for kim-jane/MCRG.  The reference has no FFI: its hot path
+ * is the C++ classes Lattice (src/lattice.hpp:5-37), IsingModel
+ * (src/ising.hpp:8-41) and MonteCarloRenormalizationGroup (src/mcrg.hpp:6-40),
+ * called from src/main.cpp:15-17 and src/rgnn.cpp:85-123.  Each entry point
+ * below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns 0 (MCRG_OK) or a negative errno-style code;
+ *     mcrg_strerror() names it.  No C++ exception crosses this ABI.
+ *   - A context owns its device memory and one CUDA stream; the caller owns
+ *     every host buffer.  Use one context per host thread.  mcrg_submit /
+ *     mcrg_poll / mcrg_wait of a server are thread-safe.
+ *   - Host lattices are int8 +-1, row-major: site (i, j) at i*L + j, i being
+ *     the first index of the reference's Lattice::spins_(i, j).
+ *   - Weight exp(-K sum_bonds s s); K < 0 is ferromagnetic (src/ising.cpp:9).
+ *
+ * Monte Carlo update.  The reference grows one Wolff cluster per sample
+ * (src/ising.cpp:87-149).  Here one "sweep" updates every site once with a
+ * checkerboard Metropolis rule: flip iff always[m] or u32 < thr[m], where
+ * m = number of anti-aligned neighbours, p[m] = min(1, exp(2K(4-2m))),
+ * always[m] = (p[m] == 1), thr[m] = floor(p[m] 2^32).  Both chains sample the
+ * same Boltzmann distribution.
+ *
+ * Random streams: Philox4x32-10, key = (seed lo32, seed hi32), counter =
+ * (row, purpose<<28 | sub<<20 | group, time, replica):
+ *   init   purpose 1, sub = colour, group = k>>7, time 0:
+ *          spin bit = bit (k&127) of the 128-bit block;
+ *   sweep  purpose 2, sub = colour, group = k>>4, time = sweep index t:
+ *          r8 = byte (k&15); purpose 3, group = k>>2: r24 = low 24 bits of
+ *          word (k&3); u32 = r8<<24 | r24;
+ *   ties   purpose 4, sub = level produced, row = ib, group = jb>>7,
+ *          time = sample index: tie value = bit (jb&127) ? +1 : -1.
+ * Site (i, j) has colour c = (i+j)&1 and split index k = j>>1.  Colour 0 is
+ * updated before colour 1 within a sweep.
+ *
+ * Coupling sums (per level, over directional offsets, periodic):
+ *   0 nn    sum_x s(x) sum_{(+-1,0),(0,+-1)} s(x+d)   (src/lattice.cpp:102-120)
+ *   1 nnn   sum_x s(x) sum_{(+-1,+-1)} s(x+d)         (src/lattice.cpp:102-120)
+ *   2 third sum_x s(x) sum_{(+-2,0),(0,+-2)} s(x+d)   (no reference counterpart)
+ *   3 plaq  sum_x s(i,j)s(i+1,j)s(i,j+1)s(i+1,j+1)     (no reference counterpart)
+ *   4 line4 sum_x s(i,j)..s(i+3,j) + s(i,j)..s(i,j+3)  (no reference counterpart)
+ * Blocking is b = 2 majority rule (src/mcrg.cpp:314-348).
+ */
+#ifndef MCRG_H_
+#define MCRG_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCRG_ABI_VERSION 1
+#define MCRG_MAX_LEVELS 14     /* L <= 32768 */
+#define MCRG_MAX_COUPLINGS 5
+#define MCRG_MAX_L 16384
+#define MCRG_SMEM_MAX_L 256    /* lattices up to this side run shared-memory resident */
+
+enum {
+  MCRG_OK = 0,
+  MCRG_ENOENT = -2,      /* unknown ticket */
+  MCRG_EIO = -5,         /* CUDA error */
+  MCRG_EAGAIN = -11,     /* not finished yet */
+  MCRG_ENOMEM = -12,     /* device or host allocation failed */
+  MCRG_EBUSY = -16,      /* server queue full */
+  MCRG_EINVAL = -22,     /* bad argument */
+  MCRG_ENOSPC = -28,     /* request exceeds the memory budget */
+  MCRG_ENOSYS = -38,     /* not supported by this build */
+  MCRG_ETIMEDOUT = -110, /* bounded wait ran out */
+  MCRG_ECANCELED = -125  /* request cancelled / server shut down */
+};
+
+typedef struct {
+  uint64_t lo;
+  int64_t hi;
+} mcrg_i128;
+
+/* Lattice(N) + IsingModel(K) + MonteCarloRenormalizationGroup(b) parameters. */
+typedef struct {
+  int32_t L;           /* lattice side N, power of two, 4..MCRG_MAX_L */
+  int32_t b;           /* block factor; 2 is the only supported value */
+  int32_t n_levels;    /* RG levels; < 0 selects log2(L)-1 (src/mcrg.cpp:43) */
+  int32_t n_couplings; /* 1..5; 2 = the reference's {nn, nnn} */
+  double K;            /* coupling */
+  uint64_t seed;       /* Philox key */
+  uint32_t replica;    /* Philox counter word 3: independent chains */
+  int32_t device;      /* CUDA device ordinal */
+} mcrg_cfg;
+
+/* Moment sums of src/mcrg.cpp:56-98 (exact integers, not averages):
+ *   S[l*MAX_C + c]             = sum_samples S_l,c
+ *   SbS[(l*MAX_C + a)*MAX_C + b]  = sum S_{l+1},a * S_l,b      (l < n_levels)
+ *   SbSb[(l*MAX_C + a)*MAX_C + b] = sum S_{l+1},a * S_{l+1},b
+ * The reference flattens the same products column-major (a + b*C). */
+typedef struct {
+  int32_t n_levels;
+  int32_t n_couplings;
+  int64_t n_samples;
+  int64_t S[(MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS];
+  mcrg_i128 SbS[MCRG_MAX_LEVELS * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS];
+  mcrg_i128 SbSb[MCRG_MAX_LEVELS * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS];
+} mcrg_moments;
+
+typedef struct mcrg_ctx mcrg_ctx;
+
+const char* mcrg_strerror(int code);
+int mcrg_abi_version(void);
+
+/* Acceptance table the sweep kernels use (host FP64, as described above). */
+int mcrg_thresholds(double K, uint32_t thr[5], uint8_t always[5]);
+
+/* Replaces `new Lattice(N)` + `new IsingModel(K)` (src/lattice.cpp:3-15,
+ * src/ising.cpp:3-11): allocates the device lattice and draws the initial
+ * +-1 coin from the init stream (src/lattice.cpp:33-41). */
+int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg);
+int mcrg_free(mcrg_ctx* ctx);
+
+/* Replaces writes / reads of the public Lattice::spins_ (src/lattice.hpp:16;
+ * read directly by src/rgnn.cpp:113-114,175).  Values must be +-1. */
+int mcrg_set_spins(mcrg_ctx* ctx, const int8_t* host_spins);
+int mcrg_get_spins(mcrg_ctx* ctx, int8_t* host_spins);
+
+/* Replaces n_sweeps calls of IsingModel::sample_new_configuration
+ * (src/ising.cpp:87-93) and IsingModel::equilibrate(lat, n, false)
+ * (src/ising.cpp:14-84). */
+int mcrg_sweep(mcrg_ctx* ctx, int64_t n_sweeps);
+
+/* Replaces `level` chained calls of block_spin_transformation
+ * (src/mcrg.cpp:314-348) on the current configuration; ties come from the
+ * tie stream at the context's next sample index, which is consumed.  Copies
+ * the (L>>level)^2 result to host_out when it is not NULL. */
+int mcrg_block(mcrg_ctx* ctx, int level, int8_t* host_out);
+
+/* Replaces Lattice::calc_interactions at every level (src/lattice.cpp:102-120,
+ * src/mcrg.cpp:78-84) for the current configuration: out[l*n_couplings + c].
+ * Consumes one sample index for the tie stream. */
+int mcrg_interactions(mcrg_ctx* ctx, int64_t* out);
+
+/* Replaces the sample loop of calc_critical_exponent (src/mcrg.cpp:72-98):
+ * n_samples x (sweeps_between sweeps, then blocking + coupling sums at every
+ * level + moment accumulation), all on the device.  `total` receives the
+ * moment sums over all samples.  When bins != NULL and bin_size > 0, bins[q]
+ * receives the sums over samples [q*bin_size, (q+1)*bin_size) for
+ * q < n_bins_cap (binned error bars). */
+int mcrg_measure(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total,
+                 int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap);
+
+/* Sweep and sample counters (the Philox time words of the next sweep / sample). */
+int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);
+/* The context's CUDA stream (cudaStream_t), for event timing. */
+int mcrg_stream(mcrg_ctx* ctx, void** stream);
+int mcrg_sync(mcrg_ctx* ctx);
+
+/* Stateless device forms of block_spin_transformation (src/mcrg.cpp:314-348)
+ * and calc_interactions (src/lattice.cpp:102-120) on a host lattice.
+ * tie_values (N/2 x N/2, +-1) gives the value of every tied block; NULL uses
+ * the tie stream (seed, replica, level, sample). */
+int mcrg_block_lattice(int32_t N, const int8_t* host_in, const int8_t* tie_values, uint64_t seed,
+                       uint32_t replica, int32_t level, uint32_t sample, int8_t* host_out, int32_t device);
+int mcrg_lattice_couplings(int32_t N, const int8_t* host_in, int32_t n_couplings, int64_t* out,
+                           int32_t device);
+
+/* ---------------------------------------------------------------------- */
+/* Batched solves: many independent chains (the reference runs one chain   */
+/* per MPI rank and sums with MPI_Allreduce, src/mcrg.cpp:101-103).         */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t L;
+  int32_t n_levels;    /* < 0: log2(L)-1 */
+  int32_t n_couplings;
+  int32_t flags;       /* reserved, 0 */
+  double K;
+  uint64_t seed;
+  uint32_t replica;
+  uint32_t pad;
+  int64_t n_eq;        /* thermalisation sweeps */
+  int64_t n_samples;   /* measurements */
+  int64_t sweeps_between;
+} mcrg_request;
+
+typedef struct {
+  int32_t status;      /* MCRG_OK or an error code */
+  int32_t pad;
+  double submit_s;     /* host clock (CLOCK_MONOTONIC seconds) at submission */
+  double done_s;       /* host clock when the result was observed complete */
+  mcrg_moments moments;
+} mcrg_result;
+
+/* Runs every request in one persistent launch on `device` (CUDA-graph
+ * captured when `use_graph` != 0) and fills results[i].  Lattices above
+ * MCRG_SMEM_MAX_L run on the tiled HBM path after the resident batch. */
+int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* results, int32_t device,
+                   int32_t use_graph);
+
+/* ---------------------------------------------------------------------- */
+/* Serving: continuous batching of MCRG requests.                          */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t device;
+  int32_t slots;            /* concurrent resident chains (CTAs) */
+  int64_t hbm_budget_bytes; /* device bytes the server may hold for lattices */
+  int32_t queue_capacity;   /* pending requests before mcrg_submit returns EBUSY */
+  int32_t pad;
+} mcrg_server_cfg;
+
+typedef struct mcrg_server mcrg_server;
+
+int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg);
+int mcrg_submit(mcrg_server* srv, const mcrg_request* req, uint64_t* ticket);
+int mcrg_poll(mcrg_server* srv, uint64_t ticket, mcrg_result* out);   /* MCRG_EAGAIN while running */
+int mcrg_wait(mcrg_server* srv, uint64_t ticket, double timeout_s, mcrg_result* out);
+int mcrg_server_stats(mcrg_server* srv, int64_t* admitted, int64_t* completed, int64_t* in_flight,
+                      int64_t* bytes_in_use);
+int mcrg_server_destroy(mcrg_server* srv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCRG_H_ */

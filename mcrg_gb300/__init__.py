@@ -1,0 +1,280 @@
+"""mcrg_gb300 -- GB300-native Monte Carlo renormalization group hot path.
+
+Python host binding of libmcrg.so (include/mcrg.h).  The compute path is the
+CUDA library; this module only marshals arguments.  The classes mirror the
+reference's host API (kim-jane/MCRG src/lattice.hpp, src/ising.hpp,
+src/mcrg.hpp) with the same names and argument meaning:
+
+    Lattice(N)                          -> mcrg_alloc
+    IsingModel(K).equilibrate(...)      -> mcrg_sweep
+    IsingModel.sample_new_configuration -> mcrg_sweep(1)
+    Lattice.calc_interactions()         -> mcrg_interactions (level 0)
+    MonteCarloRenormalizationGroup(b).calc_critical_exponent(n_eq, n, N, K)
+                                        -> mcrg_measure + host FP64 T solve
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import MCRGError, check, lib
+from .tmatrix import MomentSums, eigenvalues, jackknife, nu
+
+__all__ = ["Lattice", "IsingModel", "MonteCarloRenormalizationGroup", "MomentSums", "batch_run", "Server",
+           "block_lattice", "lattice_couplings", "thresholds", "moments_from_c", "MCRGError", "lib"]
+
+KC = -math.log(1.0 + math.sqrt(2.0)) / 2.0
+
+
+def _i128(v) -> int:
+    x = (int(v.hi) << 64) | int(v.lo)
+    return x
+
+
+def moments_from_c(m: _abi.Moments) -> MomentSums:
+    nl, Cn = int(m.n_levels), int(m.n_couplings)
+    MC = _abi.MAX_COUPLINGS
+    S = [[int(m.S[l * MC + c]) for c in range(Cn)] for l in range(nl + 1)]
+    SbS = [[[_i128(m.SbS[(l * MC + a) * MC + b]) for b in range(Cn)] for a in range(Cn)] for l in range(nl)]
+    SbSb = [[[_i128(m.SbSb[(l * MC + a) * MC + b]) for b in range(Cn)] for a in range(Cn)] for l in range(nl)]
+    return MomentSums(nl, Cn, int(m.n_samples), S, SbS, SbSb)
+
+
+def thresholds(K: float) -> tuple[np.ndarray, np.ndarray]:
+    thr = (C.c_uint32 * 5)()
+    alw = (C.c_uint8 * 5)()
+    check(lib().mcrg_thresholds(K, thr, alw), "mcrg_thresholds")
+    return np.array(list(thr), dtype=np.uint32), np.array(list(alw), dtype=np.uint8)
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Lattice:
+    """One device-resident lattice with its Markov-chain state (mcrg_ctx).
+
+    Mirrors Lattice(N) (src/lattice.cpp:3-41) plus the chain state IsingModel
+    keeps; spins cross the boundary as int8 +-1, row-major (i, j) -> i*N + j.
+    """
+
+    def __init__(self, N: int, K: float = KC, seed: int = 1, replica: int = 0, n_levels: int = -1,
+                 n_couplings: int = 2, device: int = 0, b: int = 2):
+        self._ctx = None
+        cfg = _abi.Cfg(N, b, n_levels, n_couplings, float(K), seed & 0xFFFFFFFFFFFFFFFF, replica, device)
+        h = C.c_void_p()
+        check(lib().mcrg_alloc(C.byref(h), C.byref(cfg)), "mcrg_alloc")
+        self._ctx = h
+        self.N_ = N
+        self.n_spins_ = N * N
+        self.a_ = 1
+        self.K = float(K)
+        self.n_couplings = n_couplings
+        self.n_levels = n_levels if n_levels >= 0 else int(math.log2(N)) - 1
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if self._ctx is not None and _abi._lib is not None:
+            _abi._lib.mcrg_free(self._ctx)
+        self._ctx = None
+
+    @property
+    def spins_(self) -> np.ndarray:
+        out = np.empty((self.N_, self.N_), dtype=np.int8)
+        check(lib().mcrg_get_spins(self._ctx, _ptr(out)), "mcrg_get_spins")
+        return out
+
+    @spins_.setter
+    def spins_(self, s: np.ndarray) -> None:
+        s = np.ascontiguousarray(s, dtype=np.int8)
+        if s.shape != (self.N_, self.N_):
+            raise ValueError("spins must be %dx%d" % (self.N_, self.N_))
+        check(lib().mcrg_set_spins(self._ctx, _ptr(s)), "mcrg_set_spins")
+
+    def sweep(self, n: int = 1) -> None:
+        check(lib().mcrg_sweep(self._ctx, int(n)), "mcrg_sweep")
+
+    def block(self, level: int = 1) -> np.ndarray:
+        n = self.N_ >> level
+        out = np.empty((n, n), dtype=np.int8)
+        check(lib().mcrg_block(self._ctx, int(level), _ptr(out)), "mcrg_block")
+        return out
+
+    def interactions(self) -> np.ndarray:
+        """S[level][c] of the current configuration at every level."""
+        out = (C.c_int64 * ((self.n_levels + 1) * self.n_couplings))()
+        check(lib().mcrg_interactions(self._ctx, out), "mcrg_interactions")
+        return np.array(list(out), dtype=np.int64).reshape(self.n_levels + 1, self.n_couplings)
+
+    def calc_interactions(self) -> np.ndarray:
+        """Level-0 (S_nn, S_nnn, ...) as src/lattice.cpp:102-120 returns them."""
+        return self.interactions()[0]
+
+    def measure(self, n_samples: int, sweeps_between: int = 1, bin_size: int = 0):
+        """Sample loop of src/mcrg.cpp:72-98 on the device; returns (total, bins)."""
+        tot = _abi.Moments()
+        if bin_size > 0:
+            nb = (n_samples + bin_size - 1) // bin_size
+            bins = (_abi.Moments * nb)()
+            check(lib().mcrg_measure(self._ctx, n_samples, sweeps_between, C.byref(tot), bin_size, bins, nb),
+                  "mcrg_measure")
+            return moments_from_c(tot), [moments_from_c(b) for b in bins]
+        check(lib().mcrg_measure(self._ctx, n_samples, sweeps_between, C.byref(tot), 0, None, 0), "mcrg_measure")
+        return moments_from_c(tot), []
+
+    def counters(self) -> tuple[int, int]:
+        t = C.c_uint64()
+        n = C.c_uint64()
+        check(lib().mcrg_counters(self._ctx, C.byref(t), C.byref(n)), "mcrg_counters")
+        return int(t.value), int(n.value)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().mcrg_stream(self._ctx, C.byref(s)), "mcrg_stream")
+        return int(s.value or 0)
+
+    def sync(self) -> None:
+        check(lib().mcrg_sync(self._ctx), "mcrg_sync")
+
+
+class IsingModel:
+    """IsingModel(K) (src/ising.hpp:8-41): the update rule is the device sweep."""
+
+    def __init__(self, K: float):
+        self.K_ = float(K)
+        self.P_ = 1.0 - math.exp(2.0 * K)  # kept for API parity (Wolff bond probability)
+
+    def equilibrate(self, lattice: Lattice, n_samples_eq: int, write: bool = False) -> None:
+        lattice.sweep(n_samples_eq)
+
+    def sample_new_configuration(self, lattice: Lattice) -> None:
+        lattice.sweep(1)
+
+    def calc_energy(self, lattice: Lattice) -> float:
+        return self.K_ * float(lattice.calc_interactions()[0]) / (lattice.N_ * lattice.N_)
+
+    def calc_magnetization(self, lattice: Lattice) -> float:
+        return float(lattice.spins_.astype(np.int64).sum()) / (lattice.N_ * lattice.N_)
+
+
+class MonteCarloRenormalizationGroup:
+    """MonteCarloRenormalizationGroup(b) (src/mcrg.hpp:6-40)."""
+
+    def __init__(self, b: int = 2, seed: int = 1, n_couplings: int = 2, device: int = 0, sweeps_between: int = 1):
+        if b != 2:
+            raise ValueError("only b = 2 is supported")
+        self.b_ = b
+        self.seed = seed
+        self.n_couplings = n_couplings
+        self.device = device
+        self.sweeps_between = sweeps_between
+        self.last = None
+
+    def calc_critical_exponent(self, n_samples_eq: int, n_samples: int, N: int, K: float,
+                               bin_size: int = 0, write_file: bool = False) -> list[tuple[int, float, float]]:
+        lat = Lattice(N, K, seed=self.seed, n_couplings=self.n_couplings, device=self.device)
+        try:
+            lat.sweep(n_samples_eq)
+            tot, bins = lat.measure(n_samples, self.sweeps_between, bin_size)
+        finally:
+            lat.close()
+        lams = eigenvalues(tot)
+        errs = jackknife(bins)[1] if len(bins) > 1 else [float("nan")] * len(lams)
+        rows = [(n, lam, nu(lam, self.b_)) for n, lam in enumerate(lams)]
+        self.last = (tot, bins, errs)
+        if write_file:
+            fn = "critical_exponent_N_%d_K_%s.txt" % (N, "%.7g" % K)
+            with open(fn, "w") as f:
+                f.write("# Number of parallel processes = 1\n")
+                f.write("# Number of equilibration samples = %d\n" % n_samples_eq)
+                f.write("# Number of samples = %d\n" % n_samples)
+                f.write("# %23s  %25s  %25s\n" % ("Blocking Level n", "Largest Eigenvalue", "Critical Exponent nu"))
+                for n, lam, v in rows:
+                    f.write("%25d, %25.10f, %25.10f\n" % (n, lam, v))
+        return rows
+
+
+def block_lattice(spins: np.ndarray, tie_values: np.ndarray | None = None, seed: int = 1, replica: int = 0,
+                  level: int = 1, sample: int = 0, device: int = 0) -> np.ndarray:
+    """Device b=2 majority rule (src/mcrg.cpp:314-348) on a host lattice."""
+    s = np.ascontiguousarray(spins, dtype=np.int8)
+    N = s.shape[0]
+    out = np.empty((N // 2, N // 2), dtype=np.int8)
+    tv = None if tie_values is None else np.ascontiguousarray(tie_values, dtype=np.int8)
+    check(lib().mcrg_block_lattice(N, _ptr(s), None if tv is None else _ptr(tv), seed, replica, level, sample,
+                                   _ptr(out), device), "mcrg_block_lattice")
+    return out
+
+
+def lattice_couplings(spins: np.ndarray, n_couplings: int = 5, device: int = 0) -> np.ndarray:
+    """Device coupling sums (src/lattice.cpp:102-120 and extensions) of a host lattice."""
+    s = np.ascontiguousarray(spins, dtype=np.int8)
+    out = (C.c_int64 * n_couplings)()
+    check(lib().mcrg_lattice_couplings(s.shape[0], _ptr(s), n_couplings, out, device), "mcrg_lattice_couplings")
+    return np.array(list(out), dtype=np.int64)
+
+
+def make_request(L: int, K: float, seed: int, replica: int = 0, n_eq: int = 0, n_samples: int = 0,
+                 sweeps_between: int = 1, n_levels: int = -1, n_couplings: int = 2) -> _abi.Request:
+    return _abi.Request(L, n_levels, n_couplings, 0, float(K), seed, replica, 0, n_eq, n_samples, sweeps_between)
+
+
+def batch_run(requests: list[_abi.Request], device: int = 0, use_graph: bool = True):
+    n = len(requests)
+    reqs = (_abi.Request * n)(*requests)
+    res = (_abi.Result * n)()
+    rc = lib().mcrg_batch_run(reqs, n, res, device, 1 if use_graph else 0)
+    check(rc, "mcrg_batch_run")
+    return [(int(r.status), moments_from_c(r.moments) if r.status == 0 else None) for r in res]
+
+
+class Server:
+    """Continuous-batching MCRG server (mcrg_server_*)."""
+
+    def __init__(self, device: int = 0, slots: int = 256, hbm_budget_bytes: int = 1 << 30, queue_capacity: int = 1 << 16):
+        cfg = _abi.ServerCfg(device, slots, hbm_budget_bytes, queue_capacity, 0)
+        h = C.c_void_p()
+        check(lib().mcrg_server_create(C.byref(h), C.byref(cfg)), "mcrg_server_create")
+        self._h = h
+
+    def submit(self, req: _abi.Request) -> int:
+        t = C.c_uint64()
+        rc = lib().mcrg_submit(self._h, C.byref(req), C.byref(t))
+        if rc != 0:
+            raise MCRGError(rc, "mcrg_submit")
+        return int(t.value)
+
+    def poll(self, ticket: int):
+        r = _abi.Result()
+        rc = lib().mcrg_poll(self._h, ticket, C.byref(r))
+        if rc == _abi.EAGAIN:
+            return None
+        check(rc, "mcrg_poll")
+        return r
+
+    def wait(self, ticket: int, timeout_s: float = 60.0):
+        r = _abi.Result()
+        check(lib().mcrg_wait(self._h, ticket, timeout_s, C.byref(r)), "mcrg_wait")
+        return r
+
+    def stats(self) -> dict:
+        a, c, f, b = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().mcrg_server_stats(self._h, C.byref(a), C.byref(c), C.byref(f), C.byref(b)), "mcrg_server_stats")
+        return {"admitted": a.value, "completed": c.value, "in_flight": f.value, "bytes_in_use": b.value}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            lib().mcrg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

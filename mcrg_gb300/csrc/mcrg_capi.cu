@@ -1,0 +1,538 @@
+// mcrg_capi.cu -- host side of the C ABI declared in include/mcrg.h.
+//
+// A context (mcrg_ctx) holds one lattice and its chain counters on one
+// device: lattices with L <= MCRG_SMEM_MAX_L run every sweep / measurement
+// in one shared-memory-resident CTA (mcrg_chain.cu); larger lattices live in
+// HBM and run the tiled streaming kernels (mcrg_tiled.cu).  Lattices cross
+// the ABI in natural layout (int8 +-1) and are converted on the device.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <new>
+#include <vector>
+
+#include "mcrg_internal.cuh"
+#include "mcrg_tiled.cuh"
+
+using namespace mcrg;
+
+struct mcrg_ctx {
+  mcrg_cfg cfg;
+  int n_levels;
+  cudaStream_t stream = nullptr;
+  uint8_t* d_state = nullptr;   // L*L bytes split layout (smem class)
+  TiledLattice tiled;           // HBM class
+  bool is_tiled = false;
+  uint64_t t = 0;               // next sweep index
+  uint64_t n = 0;               // next sample index
+  ChainJob* d_job = nullptr;
+  mcrg_moments* d_bins = nullptr;
+  int64_t bins_cap = 0;
+  int8_t* d_nat = nullptr;      // natural-layout staging (L*L)
+  int* d_flag = nullptr;
+  Accept acc;
+};
+
+namespace {
+
+constexpr int64_t kMaxDeviceBin = int64_t(1) << 24;  // int64 headroom of the resident accumulators
+
+int ilog2(int x) {
+  int l = 0;
+  while ((1 << l) < x) ++l;
+  return l;
+}
+
+int to_status(cudaError_t e) { return e == cudaSuccess ? MCRG_OK : MCRG_EIO; }
+
+#define CK(expr)                                  \
+  do {                                            \
+    cudaError_t _e = (expr);                      \
+    if (_e != cudaSuccess) return MCRG_EIO;       \
+  } while (0)
+
+__global__ void nat_to_split_kernel(const int8_t* __restrict__ nat, int N, uint8_t* __restrict__ split,
+                                    int* __restrict__ bad) {
+  const int half = N / 2;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N * N; s += gridDim.x * blockDim.x) {
+    const int i = s / N, j = s % N;
+    const int8_t v = nat[s];
+    if (v != 1 && v != -1) atomicOr(bad, 1);
+    split[(size_t)((i + j) & 1) * N * half + (size_t)i * half + (j >> 1)] = v > 0 ? 1 : 0;
+  }
+}
+
+__global__ void split_to_nat_kernel(const uint8_t* __restrict__ split, int N, int8_t* __restrict__ nat) {
+  const int half = N / 2;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N * N; s += gridDim.x * blockDim.x) {
+    const int i = s / N, j = s % N;
+    nat[s] = split[(size_t)((i + j) & 1) * N * half + (size_t)i * half + (j >> 1)] ? 1 : -1;
+  }
+}
+
+__global__ void nat01_kernel(const int8_t* __restrict__ nat, int n, uint8_t* __restrict__ out, int* bad) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const int8_t v = nat[s];
+    if (v != 1 && v != -1) atomicOr(bad, 1);
+    out[s] = v > 0 ? 1 : 0;
+  }
+}
+
+int grid_for(int64_t work) {
+  int64_t g = (work + 255) / 256;
+  if (g < 1) g = 1;
+  if (g > 8192) g = 8192;
+  return (int)g;
+}
+
+bool valid_L(int L) { return L >= 4 && L <= MCRG_MAX_L && (L & (L - 1)) == 0; }
+
+int resolve_levels(int L, int n_levels) {
+  const int mx = ilog2(L) - 1;
+  if (n_levels < 0) return mx;
+  return n_levels <= mx ? n_levels : -1;
+}
+
+int threads_for(int L) {
+  if (L <= 32) return 32;
+  if (L == 64) return 64;
+  if (L == 128) return 128;
+  return 256;
+}
+
+void add_moments(mcrg_moments* dst, const mcrg_moments* src) {
+  dst->n_samples += src->n_samples;
+  for (int x = 0; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; ++x) dst->S[x] += src->S[x];
+  for (int x = 0; x < MCRG_MAX_LEVELS * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS; ++x) {
+    __int128 a = ((__int128)dst->SbS[x].hi << 64) | dst->SbS[x].lo;
+    __int128 b = ((__int128)src->SbS[x].hi << 64) | src->SbS[x].lo;
+    a += b;
+    dst->SbS[x].lo = (uint64_t)a;
+    dst->SbS[x].hi = (int64_t)(a >> 64);
+    a = ((__int128)dst->SbSb[x].hi << 64) | dst->SbSb[x].lo;
+    b = ((__int128)src->SbSb[x].hi << 64) | src->SbSb[x].lo;
+    a += b;
+    dst->SbSb[x].lo = (uint64_t)a;
+    dst->SbSb[x].hi = (int64_t)(a >> 64);
+  }
+}
+
+int ensure_bins(mcrg_ctx* c, int64_t n) {
+  if (n <= c->bins_cap) return MCRG_OK;
+  if (c->d_bins) cudaFree(c->d_bins);
+  c->d_bins = nullptr;
+  c->bins_cap = 0;
+  if (cudaMalloc(&c->d_bins, sizeof(mcrg_moments) * (size_t)n) != cudaSuccess) return MCRG_ENOMEM;
+  c->bins_cap = n;
+  return MCRG_OK;
+}
+
+// Runs one resident chain job for the context and returns the device bins.
+int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_between, int64_t bin_size,
+                 int64_t* n_bins_out) {
+  ChainJob j;
+  memset(&j, 0, sizeof j);
+  j.L = c->cfg.L;
+  j.n_levels = c->n_levels;
+  j.C = c->cfg.n_couplings;
+  j.threads = threads_for(c->cfg.L);
+  j.key = Key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
+  j.replica = c->cfg.replica;
+  j.t0 = (uint32_t)c->t;
+  j.n0 = (uint32_t)c->n;
+  j.init = 0;
+  j.store = 1;
+  j.n_eq = n_eq;
+  j.n_samples = n_samples;
+  j.sweeps_between = sweeps_between;
+  j.bin_size = bin_size;
+  j.state = c->d_state;
+  j.acc = c->acc;
+  int64_t nb = n_samples > 0 ? (n_samples + bin_size - 1) / bin_size : 0;
+  if (nb > 0) {
+    int rc = ensure_bins(c, nb);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->d_bins, 0, sizeof(mcrg_moments) * (size_t)nb, c->stream));
+  }
+  j.bins = c->d_bins;
+  CK(cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream));
+  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.threads, c->stream));
+  c->t += (uint64_t)(n_eq + n_samples * sweeps_between);
+  c->n += (uint64_t)n_samples;
+  *n_bins_out = nb;
+  return MCRG_OK;
+}
+
+}  // namespace
+
+namespace mcrg {
+Accept make_accept(double K) {
+  Accept a;
+  memset(&a, 0, sizeof a);
+  uint8_t always[5];
+  mcrg_thresholds(K, a.thr, always);
+  for (int m = 0; m < 5; ++m) a.always_mask |= (uint32_t)always[m] << m;
+  a.fast = (a.always_mask == 0x1Cu) && (a.thr[1] < 0x80000000u) && (a.thr[0] <= a.thr[1]);
+  const uint32_t t0 = a.thr[0] >> 24, t1 = a.thr[1] >> 24;
+  a.cx0 = (0x80u - t0) * 0x01010101u;
+  a.cx1 = (0x80u - t1) * 0x01010101u;
+  a.cy0 = (0x7Fu - t0) * 0x01010101u;
+  a.cy1 = (0x7Fu - t1) * 0x01010101u;
+  return a;
+}
+}  // namespace mcrg
+
+extern "C" {
+
+const char* mcrg_strerror(int code) {
+  switch (code) {
+    case MCRG_OK: return "ok";
+    case MCRG_ENOENT: return "unknown ticket";
+    case MCRG_EIO: return "CUDA error";
+    case MCRG_EAGAIN: return "not finished";
+    case MCRG_ENOMEM: return "out of memory";
+    case MCRG_EBUSY: return "queue full";
+    case MCRG_EINVAL: return "invalid argument";
+    case MCRG_ENOSPC: return "request exceeds the memory budget";
+    case MCRG_ENOSYS: return "not supported";
+    case MCRG_ETIMEDOUT: return "timed out";
+    case MCRG_ECANCELED: return "cancelled";
+    default: return "unknown error";
+  }
+}
+
+int mcrg_abi_version(void) { return MCRG_ABI_VERSION; }
+
+int mcrg_thresholds(double K, uint32_t thr[5], uint8_t always[5]) {
+  if (!thr || !always || !std::isfinite(K)) return MCRG_EINVAL;
+  for (int m = 0; m < 5; ++m) {
+    const double x = 2.0 * K * (double)(4 - 2 * m);
+    if (x >= 0.0) {
+      always[m] = 1;
+      thr[m] = 0xFFFFFFFFu;
+    } else {
+      always[m] = 0;
+      thr[m] = (uint32_t)std::floor(std::exp(x) * 4294967296.0);
+    }
+  }
+  return MCRG_OK;
+}
+
+int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
+  if (!out || !cfg) return MCRG_EINVAL;
+  *out = nullptr;
+  if (!valid_L(cfg->L) || cfg->b != 2 || cfg->n_couplings < 1 || cfg->n_couplings > MCRG_MAX_COUPLINGS ||
+      !std::isfinite(cfg->K))
+    return MCRG_EINVAL;
+  const int nl = resolve_levels(cfg->L, cfg->n_levels);
+  if (nl < 0) return MCRG_EINVAL;
+  if (cfg->L <= MCRG_SMEM_MAX_L && moment_entries(nl, cfg->n_couplings) > kMaxOwned * threads_for(cfg->L))
+    return MCRG_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) return MCRG_EIO;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return MCRG_EIO;
+  mcrg_ctx* c = new (std::nothrow) mcrg_ctx();
+  if (!c) return MCRG_ENOMEM;
+  c->cfg = *cfg;
+  c->n_levels = nl;
+  c->acc = make_accept(cfg->K);
+  int rc = MCRG_OK;
+  const size_t LL = (size_t)cfg->L * cfg->L;
+  do {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = MCRG_EIO; break; }
+    if (cudaMalloc(&c->d_job, sizeof(ChainJob)) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    if (cudaMalloc(&c->d_nat, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    if (cudaMalloc(&c->d_flag, sizeof(int) * 64) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    const Key key{(uint32_t)cfg->seed, (uint32_t)(cfg->seed >> 32)};
+    if (cfg->L <= MCRG_SMEM_MAX_L) {
+      if (cudaMalloc(&c->d_state, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+      ChainJob j;
+      memset(&j, 0, sizeof j);
+      j.L = cfg->L; j.n_levels = nl; j.C = cfg->n_couplings; j.threads = threads_for(cfg->L);
+      j.key = key; j.replica = cfg->replica; j.init = 1; j.store = 1; j.bin_size = 1;
+      j.state = c->d_state; j.acc = c->acc;
+      if (cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+      if (launch_chain(c->d_job, 1, j.L, nl, j.threads, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+    } else {
+      c->is_tiled = true;
+      rc = tiled_alloc(&c->tiled, cfg->L, nl, cfg->n_couplings, key, cfg->replica, c->acc, c->stream);
+      if (rc) break;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+  } while (0);
+  if (rc) {
+    mcrg_free(c);
+    return rc;
+  }
+  *out = c;
+  return MCRG_OK;
+}
+
+int mcrg_free(mcrg_ctx* c) {
+  if (!c) return MCRG_EINVAL;
+  cudaSetDevice(c->cfg.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->is_tiled) tiled_free(&c->tiled);
+  cudaFree(c->d_state);
+  cudaFree(c->d_job);
+  cudaFree(c->d_bins);
+  cudaFree(c->d_nat);
+  cudaFree(c->d_flag);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MCRG_OK;
+}
+
+int mcrg_set_spins(mcrg_ctx* c, const int8_t* host) {
+  if (!c || !host) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int L = c->cfg.L;
+  uint8_t* dst = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  CK(cudaMemcpyAsync(c->d_nat, host, (size_t)L * L, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+  nat_to_split_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
+  CK(cudaGetLastError());
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return bad ? MCRG_EINVAL : MCRG_OK;
+}
+
+int mcrg_get_spins(mcrg_ctx* c, int8_t* host) {
+  if (!c || !host) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int L = c->cfg.L;
+  const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  split_to_nat_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(src, L, c->d_nat);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(host, c->d_nat, (size_t)L * L, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return MCRG_OK;
+}
+
+int mcrg_sweep(mcrg_ctx* c, int64_t n_sweeps) {
+  if (!c || n_sweeps < 0) return MCRG_EINVAL;
+  if (n_sweeps == 0) return MCRG_OK;
+  CK(cudaSetDevice(c->cfg.device));
+  if (c->is_tiled) {
+    int rc = tiled_sweeps(&c->tiled, (uint32_t)c->t, n_sweeps, c->stream);
+    if (rc) return rc;
+    c->t += (uint64_t)n_sweeps;
+    return MCRG_OK;
+  }
+  int64_t nb = 0;
+  return run_resident(c, n_sweeps, 0, 0, 1, &nb);
+}
+
+int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total, int64_t bin_size,
+                 mcrg_moments* bins, int64_t n_bins_cap) {
+  if (!c || n_samples < 0 || sweeps_between < 0) return MCRG_EINVAL;
+  if (bins && (bin_size <= 0 || bin_size > kMaxDeviceBin || n_bins_cap < 0)) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int nl = c->n_levels, C = c->cfg.n_couplings;
+  if (total) {
+    memset(total, 0, sizeof *total);
+    total->n_levels = nl;
+    total->n_couplings = C;
+  }
+  if (bins)
+    for (int64_t q = 0; q < n_bins_cap; ++q) {
+      memset(&bins[q], 0, sizeof bins[q]);
+      bins[q].n_levels = nl;
+      bins[q].n_couplings = C;
+    }
+  if (n_samples == 0) return MCRG_OK;
+  const int64_t dev_bin = bins ? bin_size : (n_samples < kMaxDeviceBin ? n_samples : kMaxDeviceBin);
+  std::vector<mcrg_moments> h;
+  int64_t nb = 0;
+  if (c->is_tiled) {
+    int rc = tiled_measure(&c->tiled, (uint32_t)c->t, (uint32_t)c->n, n_samples, sweeps_between, dev_bin, &nb,
+                           c->stream);
+    if (rc) return rc;
+    c->t += (uint64_t)(n_samples * sweeps_between);
+    c->n += (uint64_t)n_samples;
+    h.resize((size_t)nb);
+    CK(cudaMemcpyAsync(h.data(), tiled_bins(&c->tiled), sizeof(mcrg_moments) * (size_t)nb,
+                       cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    int rc = run_resident(c, 0, n_samples, sweeps_between, dev_bin, &nb);
+    if (rc) return rc;
+    h.resize((size_t)nb);
+    CK(cudaMemcpyAsync(h.data(), c->d_bins, sizeof(mcrg_moments) * (size_t)nb, cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  for (int64_t q = 0; q < nb; ++q) {
+    if (total) add_moments(total, &h[(size_t)q]);
+    if (bins && q < n_bins_cap) bins[q] = h[(size_t)q];
+  }
+  return MCRG_OK;
+}
+
+int mcrg_block(mcrg_ctx* c, int level, int8_t* host_out) {
+  if (!c || level < 0 || level > c->n_levels + 1 || (c->cfg.L >> level) < 2) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int L = c->cfg.L;
+  const Key key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
+  const uint32_t sample = (uint32_t)c->n;
+  c->n += 1;
+  const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  uint8_t* tmp = nullptr;
+  const size_t LL = (size_t)L * L;
+  if (cudaMalloc(&tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
+  uint8_t* buf[2] = {tmp, tmp + LL / 2};
+  const uint8_t* cur = src;
+  int n = L;
+  int rc = MCRG_OK;
+  for (int l = 0; l < level; ++l, n >>= 1) {
+    uint8_t* nxt = buf[l & 1];
+    if (launch_block_once(cur, n, nxt, nullptr, key, c->cfg.replica, l + 1, sample, c->stream) != cudaSuccess) {
+      rc = MCRG_EIO;
+      break;
+    }
+    cur = nxt;
+  }
+  if (!rc && host_out) {
+    split_to_nat_kernel<<<grid_for((int64_t)n * n), 256, 0, c->stream>>>(cur, n, c->d_nat);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(host_out, c->d_nat, (size_t)n * n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+      rc = MCRG_EIO;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
+  cudaFree(tmp);
+  return rc;
+}
+
+int mcrg_interactions(mcrg_ctx* c, int64_t* out) {
+  if (!c || !out) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int L = c->cfg.L, C = c->cfg.n_couplings, nl = c->n_levels;
+  const Key key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
+  const uint32_t sample = (uint32_t)c->n;
+  c->n += 1;
+  const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  uint8_t* tmp = nullptr;
+  int* dS = nullptr;
+  const size_t LL = (size_t)L * L;
+  if (cudaMalloc(&tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
+  if (cudaMalloc(&dS, sizeof(int) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) != cudaSuccess) {
+    cudaFree(tmp);
+    return MCRG_ENOMEM;
+  }
+  int rc = MCRG_OK;
+  uint8_t* buf[2] = {tmp, tmp + LL / 2};
+  const uint8_t* cur = src;
+  int n = L;
+  if (cudaMemsetAsync(dS, 0, sizeof(int) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS, c->stream) != cudaSuccess)
+    rc = MCRG_EIO;
+  for (int l = 0; !rc && l <= nl; ++l, n >>= 1) {
+    if (launch_couplings_once(cur, n, C, dS + l * MCRG_MAX_COUPLINGS, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+    if (l == nl) break;
+    uint8_t* nxt = buf[l & 1];
+    if (launch_block_once(cur, n, nxt, nullptr, key, c->cfg.replica, l + 1, sample, c->stream) != cudaSuccess) {
+      rc = MCRG_EIO;
+      break;
+    }
+    cur = nxt;
+  }
+  int hS[(MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS];
+  if (!rc && cudaMemcpyAsync(hS, dS, sizeof hS, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = MCRG_EIO;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
+  cudaFree(tmp);
+  cudaFree(dS);
+  if (rc) return rc;
+  for (int l = 0; l <= nl; ++l)
+    for (int cc = 0; cc < C; ++cc) out[l * C + cc] = hS[l * MCRG_MAX_COUPLINGS + cc];
+  return MCRG_OK;
+}
+
+int mcrg_counters(mcrg_ctx* c, uint64_t* sweeps, uint64_t* samples) {
+  if (!c) return MCRG_EINVAL;
+  if (sweeps) *sweeps = c->t;
+  if (samples) *samples = c->n;
+  return MCRG_OK;
+}
+
+int mcrg_stream(mcrg_ctx* c, void** stream) {
+  if (!c || !stream) return MCRG_EINVAL;
+  *stream = (void*)c->stream;
+  return MCRG_OK;
+}
+
+int mcrg_sync(mcrg_ctx* c) {
+  if (!c) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  return to_status(cudaStreamSynchronize(c->stream));
+}
+
+int mcrg_block_lattice(int32_t N, const int8_t* host_in, const int8_t* tie_values, uint64_t seed, uint32_t replica,
+                       int32_t level, uint32_t sample, int8_t* host_out, int32_t device) {
+  if (N < 2 || N > MCRG_MAX_L || (N & (N - 1)) || !host_in || !host_out || level < 1 || level > 255)
+    return MCRG_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return MCRG_EIO;
+  const size_t NN = (size_t)N * N, HH = NN / 4;
+  int8_t* d_nat = nullptr;
+  uint8_t *d_split = nullptr, *d_out = nullptr, *d_tie = nullptr;
+  int* d_bad = nullptr;
+  int rc = MCRG_OK;
+  if (cudaMalloc(&d_nat, NN) != cudaSuccess || cudaMalloc(&d_split, NN) != cudaSuccess ||
+      cudaMalloc(&d_out, HH + 16) != cudaSuccess || cudaMalloc(&d_tie, HH + 16) != cudaSuccess ||
+      cudaMalloc(&d_bad, sizeof(int)) != cudaSuccess)
+    rc = MCRG_ENOMEM;
+  cudaStream_t s = 0;
+  if (!rc) {
+    cudaMemsetAsync(d_bad, 0, sizeof(int), s);
+    cudaMemcpyAsync(d_nat, host_in, NN, cudaMemcpyHostToDevice, s);
+    nat_to_split_kernel<<<grid_for((int64_t)NN), 256, 0, s>>>(d_nat, N, d_split, d_bad);
+    const uint8_t* tie = nullptr;
+    if (tie_values) {
+      cudaMemcpyAsync(d_nat, tie_values, HH, cudaMemcpyHostToDevice, s);
+      nat01_kernel<<<grid_for((int64_t)HH), 256, 0, s>>>(d_nat, (int)HH, d_tie, d_bad);
+      tie = d_tie;
+    }
+    const Key key{(uint32_t)seed, (uint32_t)(seed >> 32)};
+    launch_block_once(d_split, N, d_out, tie, key, replica, level, sample, s);
+    split_to_nat_kernel<<<grid_for((int64_t)HH), 256, 0, s>>>(d_out, N / 2, d_nat);
+    cudaMemcpyAsync(host_out, d_nat, HH, cudaMemcpyDeviceToHost, s);
+    int bad = 0;
+    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = MCRG_EIO;
+    else if (bad) rc = MCRG_EINVAL;
+  }
+  cudaFree(d_nat); cudaFree(d_split); cudaFree(d_out); cudaFree(d_tie); cudaFree(d_bad);
+  return rc;
+}
+
+int mcrg_lattice_couplings(int32_t N, const int8_t* host_in, int32_t n_couplings, int64_t* out, int32_t device) {
+  if (N < 2 || N > MCRG_MAX_L || (N & (N - 1)) || !host_in || !out || n_couplings < 1 ||
+      n_couplings > MCRG_MAX_COUPLINGS)
+    return MCRG_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return MCRG_EIO;
+  const size_t NN = (size_t)N * N;
+  int8_t* d_nat = nullptr;
+  uint8_t* d_split = nullptr;
+  int* d_S = nullptr;
+  int rc = MCRG_OK;
+  if (cudaMalloc(&d_nat, NN) != cudaSuccess || cudaMalloc(&d_split, NN) != cudaSuccess ||
+      cudaMalloc(&d_S, sizeof(int) * 8) != cudaSuccess)
+    rc = MCRG_ENOMEM;
+  if (!rc) {
+    cudaStream_t s = 0;
+    cudaMemsetAsync(d_S, 0, sizeof(int) * 8, s);
+    cudaMemcpyAsync(d_nat, host_in, NN, cudaMemcpyHostToDevice, s);
+    nat_to_split_kernel<<<grid_for((int64_t)NN), 256, 0, s>>>(d_nat, N, d_split, d_S + 7);
+    launch_couplings_once(d_split, N, n_couplings, d_S, s);
+    int h[8];
+    cudaMemcpyAsync(h, d_S, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = MCRG_EIO;
+    else if (h[7]) rc = MCRG_EINVAL;
+    else
+      for (int c = 0; c < n_couplings; ++c) out[c] = h[c];
+  }
+  cudaFree(d_nat); cudaFree(d_split); cudaFree(d_S);
+  return rc;
+}
+
+}  // extern "C"

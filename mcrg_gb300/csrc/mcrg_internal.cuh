@@ -1,0 +1,72 @@
+// mcrg_internal.cuh -- job descriptors and launchers shared by the CUDA
+// translation units of libmcrg.  Not part of the public ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/mcrg.h"
+#include "mcrg_device.cuh"
+
+namespace mcrg {
+
+// One independent Markov chain run shared-memory resident by one CTA.
+struct ChainJob {
+  int32_t L, n_levels, C, threads;
+  Key key;
+  uint32_t replica;
+  uint32_t t0;        // Philox time of the first sweep
+  uint32_t n0;        // Philox time (sample index) of the first measurement
+  uint32_t init;      // 1: draw the initial coin; 0: load `state`
+  uint32_t store;     // 1: write the final configuration back to `state`
+  int64_t n_eq, n_samples, sweeps_between, bin_size;
+  uint8_t* state;     // L*L bytes: colour-0 array then colour-1 array
+  mcrg_moments* bins; // ceil(n_samples / bin_size) outputs, zeroed by the host
+  Accept acc;
+};
+
+// Shared-memory plan of a resident lattice and its blocked levels.
+struct SmemPlan {
+  int off[MCRG_MAX_LEVELS + 2];
+  int s_off;    // int32 S[(MCRG_MAX_LEVELS+1) * MCRG_MAX_COUPLINGS]
+  int q_off;    // int32 qcount[2], then uint32 queue[qcap]
+  int qcap;
+  int bytes;
+};
+
+__host__ __device__ inline SmemPlan make_plan(int L, int n_levels) {
+  SmemPlan p;
+  int off = 0, n = L;
+  for (int l = 0; l <= n_levels; ++l, n >>= 1) {
+    p.off[l] = off;
+    off += ((n * n + 15) / 16) * 16;
+  }
+  p.s_off = off;
+  off += ((MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS * 4 + 15) / 16 * 16;
+  p.q_off = off;
+  int qcap = (L * L) / 64;
+  if (qcap < 64) qcap = 64;
+  p.qcap = qcap;
+  off += 16 + qcap * 4;
+  p.bytes = (off + 15) / 16 * 16;
+  return p;
+}
+
+// Largest number of moment entries one thread owns in the chain kernel.
+constexpr int kMaxOwned = 8;
+
+inline int moment_entries(int n_levels, int C) { return (n_levels + 1) * C + 2 * n_levels * C * C; }
+
+// Host: acceptance parameters for coupling K (FP64, see include/mcrg.h).
+Accept make_accept(double K);
+
+// Launch `n_jobs` chains (all with the same L, n_levels and threads).
+cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int threads,
+                         cudaStream_t stream);
+
+// Stateless helpers on a device lattice in split layout (used by
+// mcrg_block_lattice / mcrg_lattice_couplings and the HBM path's tail).
+cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat,
+                              Key key, uint32_t replica, int level, uint32_t sample, cudaStream_t s);
+cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out, cudaStream_t s);
+
+}  // namespace mcrg

@@ -1,0 +1,342 @@
+// mcrg_ops.cuh -- per-chunk device routines shared by the resident chain
+// kernel (mcrg_chain.cu) and the HBM-tiled kernels (mcrg_tiled.cu): the
+// initial coin, the SWAR checkerboard update of a chunk, deferred tie
+// resolution, the coupling sums of one level and b=2 majority-rule blocking.
+// Every routine takes plain pointers, so the same code runs on shared or
+// global memory.
+#pragma once
+#include "mcrg_internal.cuh"
+
+namespace mcrg {
+namespace {
+
+__device__ __forceinline__ void load_words4(const uint8_t* p, uint32_t (&w)[4]) {
+  const uint4 v = *reinterpret_cast<const uint4*>(p);
+  w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+}
+__device__ __forceinline__ void load_words2(const uint8_t* p, uint32_t (&w)[2]) {
+  const uint2 v = *reinterpret_cast<const uint2*>(p);
+  w[0] = v.x; w[1] = v.y;
+}
+template <int NW>
+__device__ __forceinline__ void load_words(const uint8_t* p, uint32_t (&w)[NW]) {
+  if constexpr (NW == 4) load_words4(p, w); else load_words2(p, w);
+}
+template <int NW>
+__device__ __forceinline__ void store_words(uint8_t* p, const uint32_t (&w)[NW]) {
+  if constexpr (NW == 4) *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+  else *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+}
+__device__ __forceinline__ uint32_t load_word(const uint8_t* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// Tie entry: row << 14 | k << 1 | m (m in {0,1}); row < 2^18, k < 8192.
+__device__ __forceinline__ uint32_t tie_entry(int i, int k, uint32_t m) {
+  return ((uint32_t)i << 14) | ((uint32_t)k << 1) | (m & 1u);
+}
+
+__device__ __forceinline__ bool resolve_tie(Key key, uint32_t replica, int c, int i, int k, uint32_t m,
+                                            uint32_t t, const Accept& a) {
+  const uint4 lo = stream_block(key, replica, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
+  const uint32_t r24 = u4get(lo, k & 3) & 0xFFFFFFu;
+  return r24 < (a.thr[m] & 0xFFFFFFu);
+}
+
+// ---------------------------------------------------------------------------
+// Initial coin (P_INIT): spin bit of (colour c, row i, k) = bit (k&127) of
+// the block (row i, group k>>7, sub c, time 0).
+// ---------------------------------------------------------------------------
+__device__ void init_level0(uint8_t* lat, int L, Key key, uint32_t rep, int tid, int T) {
+  const int half = L / 2;
+  if (half >= 16) {
+    const int cpr = half / 16;
+    for (int task = tid; task < 2 * L * cpr; task += T) {
+      const int c = task / (L * cpr), rem = task % (L * cpr), i = rem / cpr, k0 = (rem % cpr) * 16;
+      const uint4 b = stream_block(key, rep, P_INIT, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 7), 0u);
+      const uint32_t bits = (u4get(b, (k0 & 127) >> 5) >> (k0 & 31)) & 0xFFFFu;
+      *reinterpret_cast<uint4*>(lat + (size_t)c * L * half + (size_t)i * half + k0) =
+          make_uint4(spread4(bits), spread4(bits >> 4), spread4(bits >> 8), spread4(bits >> 12));
+    }
+  } else {
+    for (int s = tid; s < 2 * L * half; s += T) {
+      const int c = s / (L * half), rem = s % (L * half), i = rem / half, k = rem % half;
+      const uint4 b = stream_block(key, rep, P_INIT, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 7), 0u);
+      lat[(size_t)c * L * half + (size_t)i * half + k] = (uint8_t)((u4get(b, (k & 127) >> 5) >> (k & 31)) & 1u);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SWAR update of one chunk of NW words of colour c.  tw: the chunk; uw/dw:
+// the other colour's chunks in the rows above / below; mw: the other colour's
+// chunk in the same row; e: the byte just past the chunk (q = 1) or just
+// before it (q = 0) in that row; R: the chunk's P_SWEEP_HI block.  Writes
+// the updated words to nw and the open (tied) bytes to ties; returns their OR.
+// ---------------------------------------------------------------------------
+template <int NW>
+__device__ __forceinline__ uint32_t chunk_update(const uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
+                                                 const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t e,
+                                                 uint32_t q, const uint4& R, const Accept& a, uint32_t (&nw)[NW],
+                                                 uint32_t (&ties)[NW]) {
+  uint32_t tie_any = 0;
+#pragma unroll
+  for (int j = 0; j < NW; ++j) {
+    // side neighbour: O[i][k+1] when q = 1, O[i][k-1] when q = 0
+    const uint32_t nxt = (j + 1 < NW) ? mw[j + 1] : e;
+    const uint32_t prv = (j > 0) ? mw[j - 1] : (e << 24);
+    const uint32_t side = q ? __funnelshift_r(mw[j], nxt, 8) : __funnelshift_r(prv, mw[j], 24);
+    nw[j] = swar_update(tw[j], uw[j], dw[j], mw[j], side, u4get(R, j), a, &ties[j]);
+    tie_any |= ties[j];
+  }
+  return tie_any;
+}
+
+// Queues (or, when the queue is full, resolves in place) the open sites of
+// a chunk.  ent(k) gives the queue entry of chunk byte k (k = 4j + byte);
+// resolve(k, m) gives the exact decision for that byte.
+template <int NW, class Ent, class Res>
+__device__ __forceinline__ void queue_ties(const uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
+                                           const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t e,
+                                           uint32_t q, const uint32_t (&ties)[NW], uint32_t (&nw)[NW],
+                                           int* qcount, uint32_t* queue, int qcap, Ent ent, Res resolve) {
+#pragma unroll
+  for (int j = 0; j < NW; ++j) {
+    uint32_t tb = ties[j];
+    while (tb) {
+      const int byte = (__ffs(tb) - 1) >> 3;
+      tb &= tb - 1;
+      const uint32_t nxt = (j + 1 < NW) ? mw[j + 1] : e;
+      const uint32_t prv = (j > 0) ? mw[j - 1] : (e << 24);
+      const uint32_t side = q ? __funnelshift_r(mw[j], nxt, 8) : __funnelshift_r(prv, mw[j], 24);
+      const uint32_t m = (swar_m(tw[j], uw[j], dw[j], mw[j], side) >> (8 * byte)) & 0xFFu;
+      const int slot = atomicAdd(qcount, 1);
+      if (slot < qcap) queue[slot] = ent(4 * j + byte, m);
+      else if (resolve(4 * j + byte, m)) nw[j] ^= 1u << (8 * byte);
+    }
+  }
+}
+
+// Vector sweep of colour c on an n x n resident lattice (n >= 16).
+template <int NW>
+__device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
+                                 const Accept& a, int* qcount, uint32_t* queue, int qcap, int tid, int T) {
+  constexpr int CB = 4 * NW;  // chunk bytes
+  const int half = n / 2, cpr = half / CB;
+  uint8_t* Cc = lat + (size_t)c * n * half;
+  const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
+  for (int task = tid; task < n * cpr; task += T) {
+    const int i = task / cpr, k0 = (task % cpr) * CB;
+    const uint32_t q = (uint32_t)((i + c) & 1);
+    uint8_t* tp = Cc + (size_t)i * half + k0;
+    uint32_t tw[NW], uw[NW], dw[NW], mw[NW];
+    load_words<NW>(tp, tw);
+    load_words<NW>(Oc + (size_t)((i - 1) & (n - 1)) * half + k0, uw);
+    load_words<NW>(Oc + (size_t)((i + 1) & (n - 1)) * half + k0, dw);
+    load_words<NW>(Oc + (size_t)i * half + k0, mw);
+    const uint32_t e = Oc[(size_t)i * half + ((q ? (k0 + CB) : (k0 - 1)) & (half - 1))];
+    const uint4 R = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 4), t);
+    uint32_t nw[NW], ties[NW];
+    if (chunk_update<NW>(tw, uw, dw, mw, e, q, R, a, nw, ties)) {
+      queue_ties<NW>(tw, uw, dw, mw, e, q, ties, nw, qcount, queue, qcap,
+                     [&](int kb, uint32_t m) { return tie_entry(i, k0 + kb, m); },
+                     [&](int kb, uint32_t m) { return resolve_tie(key, rep, c, i, k0 + kb, m, t, a); });
+    }
+    store_words<NW>(tp, nw);
+  }
+}
+
+__device__ void resolve_queue(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep, const Accept& a,
+                              int count, const uint32_t* queue, int qcap, int tid, int T) {
+  const int half = n / 2;
+  uint8_t* Cc = lat + (size_t)c * n * half;
+  const int cnt = count < qcap ? count : qcap;
+  for (int e = tid; e < cnt; e += T) {
+    const uint32_t v = queue[e];
+    const int i = (int)(v >> 14), k = (int)((v >> 1) & 0x1FFFu);
+    const uint32_t m = v & 1u;
+    if (resolve_tie(key, rep, c, i, k, m, t, a)) Cc[(size_t)i * half + k] ^= 1u;
+  }
+}
+
+// Scalar sweep of colour c (any n >= 4, any K): exact 32-bit draw per site.
+__device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
+                                    const Accept& a, int tid, int T) {
+  const int half = n / 2;
+  uint8_t* Cc = lat + (size_t)c * n * half;
+  const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
+  for (int s = tid; s < n * half; s += T) {
+    const int i = s / half, k = s % half, q = (i + c) & 1;
+    const uint32_t tv = Cc[(size_t)i * half + k];
+    const uint32_t m = (Oc[(size_t)((i - 1) & (n - 1)) * half + k] != tv) +
+                       (Oc[(size_t)((i + 1) & (n - 1)) * half + k] != tv) +
+                       (Oc[(size_t)i * half + ((k - 1 + q) & (half - 1))] != tv) +
+                       (Oc[(size_t)i * half + ((k + q) & (half - 1))] != tv);
+    bool flip;
+    if ((a.always_mask >> m) & 1u) {
+      flip = true;
+    } else {
+      const uint4 hi = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 4), t);
+      const uint4 lo = stream_block(key, rep, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
+      const uint32_t r8 = (u4get(hi, (k & 15) >> 2) >> (8 * (k & 3))) & 0xFFu;
+      const uint32_t u32 = (r8 << 24) | (u4get(lo, k & 3) & 0xFFFFFFu);
+      flip = u32 < a.thr[m];
+    }
+    if (flip) Cc[(size_t)i * half + k] = (uint8_t)(tv ^ 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Coupling sums of one level.  Per site, downward / rightward forms of the
+// directional sums (each symmetric pair counted twice, as src/lattice.cpp
+// counts every bond from both ends).  Accumulates final values in acc[5].
+// ---------------------------------------------------------------------------
+template <int NW>
+__device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&acc)[5]) {
+  constexpr int CB = 4 * NW;
+  const int half = n / 2, cpr = half / CB;
+  for (int task = tid; task < 2 * n * cpr; task += T) {
+    const int c = task / (n * cpr), rem = task % (n * cpr), i = rem / cpr, k0 = (rem % cpr) * CB;
+    const uint32_t q = (uint32_t)((i + c) & 1);
+    const uint8_t* C = lev + (size_t)c * n * half;
+    const uint8_t* O = lev + (size_t)(1 - c) * n * half;
+    const uint8_t* Ci = C + (size_t)i * half;
+    const uint8_t* Cd = C + (size_t)((i + 1) & (n - 1)) * half;
+    const uint8_t* Cd2 = C + (size_t)((i + 2) & (n - 1)) * half;
+    const uint8_t* Oi = O + (size_t)i * half;
+    const uint8_t* Od = O + (size_t)((i + 1) & (n - 1)) * half;
+    const uint8_t* Od3 = O + (size_t)((i + 3) & (n - 1)) * half;
+    uint32_t ci[NW], cd[NW], cd2[NW], oi[NW], od[NW], od3[NW];
+    load_words<NW>(Ci + k0, ci);
+    load_words<NW>(Cd + k0, cd);
+    load_words<NW>(Cd2 + k0, cd2);
+    load_words<NW>(Oi + k0, oi);
+    load_words<NW>(Od + k0, od);
+    load_words<NW>(Od3 + k0, od3);
+    const int kn = (k0 + CB) & (half - 1), kp = (k0 - 4) & (half - 1);
+    const uint32_t ci_n = load_word(Ci + kn), oi_n = load_word(Oi + kn);
+    const uint32_t cd_n = load_word(Cd + kn), cd_p = load_word(Cd + kp);
+    uint32_t a = 0, b = 0, e = 0, p = 0, h = 0;
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+      const uint32_t ci_nx = (j + 1 < NW) ? ci[j + 1] : ci_n;
+      const uint32_t oi_nx = (j + 1 < NW) ? oi[j + 1] : oi_n;
+      const uint32_t cd_nx = (j + 1 < NW) ? cd[j + 1] : cd_n;
+      const uint32_t cd_pv = (j > 0) ? cd[j - 1] : cd_p;
+      const uint32_t ci1 = __funnelshift_r(ci[j], ci_nx, 8);             // C[i][k+1]
+      const uint32_t oiq = __funnelshift_r(oi[j], oi_nx, 8 * q);         // O[i][k+q]
+      const uint32_t oiq1 = __funnelshift_rc(oi[j], oi_nx, 8 * q + 8);   // O[i][k+q+1]
+      const uint32_t cdq = __funnelshift_r(cd[j], cd_nx, 8 * q);         // C[i+1][k+q]
+      const uint32_t cdqm = __funnelshift_rc(cd_pv, cd[j], 24 + 8 * q);  // C[i+1][k+q-1]
+      const uint32_t x = ci[j];
+      a += (x ^ od[j]) + (x ^ oiq);
+      b += (x ^ cdq) + (x ^ cdqm);
+      e += (x ^ cd2[j]) + (x ^ ci1);
+      p += x ^ od[j] ^ oiq ^ cdq;
+      h += (x ^ oiq ^ ci1 ^ oiq1) + (x ^ od[j] ^ cd2[j] ^ od3[j]);
+    }
+    acc[0] += 4 * CB - 4 * (int)bytesum(a);
+    acc[1] += 4 * CB - 4 * (int)bytesum(b);
+    acc[2] += 4 * CB - 4 * (int)bytesum(e);
+    acc[3] += CB - 2 * (int)bytesum(p);
+    acc[4] += 2 * CB - 2 * (int)bytesum(h);
+  }
+}
+
+__device__ __forceinline__ int spin_at(const uint8_t* lev, int n, int i, int j) {
+  i &= n - 1;
+  j &= n - 1;
+  const int half = n / 2;
+  return 2 * (int)lev[(size_t)((i + j) & 1) * n * half + (size_t)i * half + (j >> 1)] - 1;
+}
+
+// Direct directional sums (any n >= 2), one site per thread-iteration.
+__device__ void couplings_scalar(const uint8_t* lev, int n, int tid, int T, int (&acc)[5]) {
+  for (int s = tid; s < n * n; s += T) {
+    const int i = s / n, j = s % n;
+    const int v = spin_at(lev, n, i, j);
+    acc[0] += v * (spin_at(lev, n, i + 1, j) + spin_at(lev, n, i - 1, j) + spin_at(lev, n, i, j + 1) +
+                   spin_at(lev, n, i, j - 1));
+    acc[1] += v * (spin_at(lev, n, i + 1, j + 1) + spin_at(lev, n, i - 1, j + 1) +
+                   spin_at(lev, n, i + 1, j - 1) + spin_at(lev, n, i - 1, j - 1));
+    acc[2] += v * (spin_at(lev, n, i + 2, j) + spin_at(lev, n, i - 2, j) + spin_at(lev, n, i, j + 2) +
+                   spin_at(lev, n, i, j - 2));
+    acc[3] += v * spin_at(lev, n, i + 1, j) * spin_at(lev, n, i, j + 1) * spin_at(lev, n, i + 1, j + 1);
+    acc[4] += v * spin_at(lev, n, i + 1, j) * spin_at(lev, n, i + 2, j) * spin_at(lev, n, i + 3, j) +
+              v * spin_at(lev, n, i, j + 1) * spin_at(lev, n, i, j + 2) * spin_at(lev, n, i, j + 3);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// b = 2 majority rule, level n -> n/2.  Block (ib, jb) sums colour arrays
+// B[2ib][jb] + W[2ib][jb] + B[2ib+1][jb] + W[2ib+1][jb] (same split column
+// jb in all four rows).  Output (ib, jb) has colour (ib+jb)&1, index jb>>1.
+// tie_nat (optional): natural-layout (n/2)^2 bytes, 1 = +1, 0 = -1.
+// ---------------------------------------------------------------------------
+__device__ void block_vec(const uint8_t* in, int n, uint8_t* out, const uint8_t* tie_nat, Key key,
+                          uint32_t rep, int level_out, uint32_t sample, int tid, int T) {
+  const int half = n / 2, hn = n / 2, ohalf = hn / 2, cpr = hn / 16;
+  const uint8_t* B = in;
+  const uint8_t* W = in + (size_t)n * half;
+  for (int task = tid; task < hn * cpr; task += T) {
+    const int ib = task / cpr, jb0 = (task % cpr) * 16;
+    uint32_t b0[4], w0[4], b1[4], w1[4];
+    load_words4(B + (size_t)(2 * ib) * half + jb0, b0);
+    load_words4(W + (size_t)(2 * ib) * half + jb0, w0);
+    load_words4(B + (size_t)(2 * ib + 1) * half + jb0, b1);
+    load_words4(W + (size_t)(2 * ib + 1) * half + jb0, w1);
+    uint32_t tb[4];
+    if (tie_nat) {
+      load_words4(tie_nat + (size_t)ib * hn + jb0, tb);
+    } else {
+      const uint4 r = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(jb0 >> 7), sample);
+      const uint32_t bits = (u4get(r, (jb0 & 127) >> 5) >> (jb0 & 31)) & 0xFFFFu;
+      tb[0] = spread4(bits); tb[1] = spread4(bits >> 4); tb[2] = spread4(bits >> 8); tb[3] = spread4(bits >> 12);
+    }
+    uint32_t res[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t s = b0[j] + w0[j] + b1[j] + w1[j];  // up spins per block, 0..4
+      const uint32_t g3 = s + 0x7D7D7D7Du, g2 = s + 0x7E7E7E7Eu;
+      res[j] = ((g3 >> 7) & 0x01010101u) | (((g2 & ~g3) >> 7) & tb[j] & 0x01010101u);
+    }
+    const uint32_t e0 = __byte_perm(res[0], res[1], 0x6420), e1 = __byte_perm(res[2], res[3], 0x6420);
+    const uint32_t o0 = __byte_perm(res[0], res[1], 0x7531), o1 = __byte_perm(res[2], res[3], 0x7531);
+    const int ce = ib & 1;
+    *reinterpret_cast<uint2*>(out + (size_t)ce * hn * ohalf + (size_t)ib * ohalf + (jb0 >> 1)) = make_uint2(e0, e1);
+    *reinterpret_cast<uint2*>(out + (size_t)(1 - ce) * hn * ohalf + (size_t)ib * ohalf + (jb0 >> 1)) =
+        make_uint2(o0, o1);
+  }
+}
+
+__device__ void block_scalar(const uint8_t* in, int n, uint8_t* out, const uint8_t* tie_nat, Key key,
+                             uint32_t rep, int level_out, uint32_t sample, int tid, int T) {
+  const int hn = n / 2, ohalf = hn / 2 > 0 ? hn / 2 : 1;
+  for (int s = tid; s < hn * hn; s += T) {
+    const int ib = s / hn, jb = s % hn;
+    const int tot = spin_at(in, n, 2 * ib, 2 * jb) + spin_at(in, n, 2 * ib, 2 * jb + 1) +
+                    spin_at(in, n, 2 * ib + 1, 2 * jb) + spin_at(in, n, 2 * ib + 1, 2 * jb + 1);
+    uint32_t v;
+    if (tot > 0) v = 1;
+    else if (tot < 0) v = 0;
+    else if (tie_nat) v = tie_nat[(size_t)ib * hn + jb];
+    else {
+      const uint4 r = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(jb >> 7), sample);
+      v = (u4get(r, (jb & 127) >> 5) >> (jb & 31)) & 1u;
+    }
+    out[(size_t)((ib + jb) & 1) * hn * ohalf + (size_t)ib * ohalf + (jb >> 1)] = (uint8_t)v;
+  }
+}
+
+__device__ __forceinline__ void reduce_into(int (&acc)[5], int* S, int C) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    const int v = __reduce_add_sync(0xFFFFFFFFu, acc[c]);
+    if (lane == 0 && c < C) atomicAdd(&S[c], v);
+  }
+}
+
+__device__ __forceinline__ void sync_group() { __syncthreads(); }
+
+
+}  // namespace
+}  // namespace mcrg

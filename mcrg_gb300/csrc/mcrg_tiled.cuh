@@ -1,0 +1,37 @@
+// mcrg_tiled.cuh -- HBM-resident lattices (MCRG_SMEM_MAX_L < L <= MCRG_MAX_L).
+#pragma once
+#include "mcrg_internal.cuh"
+
+namespace mcrg {
+
+struct TiledLattice {
+  int L = 0, nl = 0, C = 0;
+  Key key{0, 0};
+  uint32_t replica = 0;
+  Accept acc{};
+  uint8_t* buf[2] = {nullptr, nullptr};  // ping-pong level-0 configurations
+  int cur = 0;
+  uint8_t* levels = nullptr;             // blocked levels 1..n_hbm (HBM-resident sizes) + tail level
+  size_t level_off[MCRG_MAX_LEVELS + 2] = {};
+  int n_hbm = 0;                          // levels 0..n_hbm-1 are measured from HBM; level n_hbm by the tail CTA
+  unsigned long long* d_S = nullptr;      // per-sample coupling sums [(nl+1)*5] (int64)
+  int* d_status = nullptr;                // kernel error flags
+  mcrg_moments* d_bins = nullptr;
+  int64_t bins_cap = 0;
+  int tile_rows = 32, tile_cols = 1024, ctas = 0;
+};
+
+int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica, const Accept& acc,
+                cudaStream_t s);
+void tiled_free(TiledLattice* t);
+uint8_t* tiled_state(TiledLattice* t);
+// n sweeps starting at sweep index t0 (one fused two-colour pass per sweep).
+int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s);
+// n_samples x (sweeps_between sweeps + measurement); bins of bin_size samples.
+int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, int64_t sweeps_between,
+                  int64_t bin_size, int64_t* n_bins, cudaStream_t s);
+mcrg_moments* tiled_bins(TiledLattice* t);
+// Device error flags raised by the tiled kernels (0 = none).
+int tiled_status(TiledLattice* t, cudaStream_t s);
+
+}  // namespace mcrg

@@ -1,0 +1,203 @@
+"""ctypes wrapper of the CPU oracle (oracle/mcrg_oracle.c) and of the
+reference harness (oracle/_ref/libmcrg_ref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline / reference legs, never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+P = C.POINTER
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        h = C.CDLL(path)
+        h.orc_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
+        h.orc_thresholds.argtypes = [C.c_double, P(C.c_uint32), P(C.c_uint8)]
+        h.orc_init_spins.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_void_p]
+        h.orc_sweep.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int64]
+        h.orc_block.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_uint64,
+                                C.c_uint32, C.c_int, C.c_uint32]
+        h.orc_block.restype = C.c_int
+        h.orc_couplings.argtypes = [C.c_int, C.c_void_p, C.c_int, P(C.c_int64)]
+        h.orc_chain.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_uint64, C.c_uint32, C.c_int, C.c_void_p,
+                                C.c_uint32, C.c_uint32, C.c_int64, C.c_int64, C.c_int64, C.c_void_p]
+        h.orc_chain.restype = C.c_int
+        h.orc_wolff_chain.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_uint64, C.c_void_p, C.c_int64,
+                                      C.c_int64, C.c_void_p]
+        h.orc_wolff_chain.restype = C.c_int64
+        h.orc_exact4.argtypes = [C.c_double, C.c_int, P(C.c_double)]
+        h.orc_wolff_new.argtypes = [C.c_int, C.c_double, C.c_uint64]
+        h.orc_wolff_new.restype = C.c_void_p
+        h.orc_wolff_free.argtypes = [C.c_void_p]
+        h.orc_wolff_steps.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        h.orc_wolff_steps.restype = C.c_int64
+        h.orc_measure.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint32, C.c_uint32,
+                                  P(C.c_int64)]
+        h.orc_measure.restype = C.c_int
+        _lib = h
+    return _lib
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def philox(ctr, key) -> list[int]:
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def thresholds(K: float):
+    thr = (C.c_uint32 * 5)()
+    alw = (C.c_uint8 * 5)()
+    lib().orc_thresholds(K, thr, alw)
+    return np.array(list(thr), dtype=np.uint32), np.array(list(alw), dtype=np.uint8)
+
+
+def init_spins(N: int, seed: int, replica: int = 0) -> np.ndarray:
+    s = np.empty((N, N), dtype=np.int8)
+    lib().orc_init_spins(N, seed, replica, _p(s))
+    return s
+
+
+def sweep(spins: np.ndarray, K: float, seed: int, replica: int = 0, t0: int = 0, n: int = 1) -> np.ndarray:
+    s = np.ascontiguousarray(spins, dtype=np.int8).copy()
+    lib().orc_sweep(s.shape[0], _p(s), K, seed, replica, t0, n)
+    return s
+
+
+def block(spins: np.ndarray, tie_vals=None, seed: int = 1, replica: int = 0, level: int = 1, sample: int = 0):
+    """(blocked lattice, number of ties).  tie_vals: sequence consumed in
+    ib-outer order (reference semantics); None: the Philox tie stream."""
+    s = np.ascontiguousarray(spins, dtype=np.int8)
+    N = s.shape[0]
+    out = np.empty((N // 2, N // 2), dtype=np.int8)
+    if tie_vals is None:
+        n = lib().orc_block(N, _p(s), _p(out), 1, None, 0, seed, replica, level, sample)
+    else:
+        tv = np.ascontiguousarray(tie_vals, dtype=np.int8)
+        n = lib().orc_block(N, _p(s), _p(out), 0, _p(tv), len(tv), seed, replica, level, sample)
+    return out, n
+
+
+def couplings(spins: np.ndarray, C_: int = 5) -> np.ndarray:
+    s = np.ascontiguousarray(spins, dtype=np.int8)
+    out = (C.c_int64 * C_)()
+    lib().orc_couplings(s.shape[0], _p(s), C_, out)
+    return np.array(list(out), dtype=np.int64)
+
+
+def chain(N: int, K: float, C_: int, n_levels: int, seed: int, replica: int = 0, n_eq: int = 0,
+          n_samples: int = 0, sweeps_between: int = 1, spins: np.ndarray | None = None, t0: int = 0, n0: int = 0):
+    """(S trace [n_samples][n_levels+1][C], final spins) of the device chain's restatement."""
+    s = np.empty((N, N), dtype=np.int8) if spins is None else np.ascontiguousarray(spins, dtype=np.int8).copy()
+    tr = np.zeros((max(n_samples, 1), n_levels + 1, C_), dtype=np.int64)
+    rc = lib().orc_chain(N, K, C_, n_levels, seed, replica, 0 if spins is None else 1, _p(s), t0, n0, n_eq,
+                         n_samples, sweeps_between, _p(tr))
+    if rc != 0:
+        raise RuntimeError("orc_chain failed: %d" % rc)
+    return tr[:n_samples], s
+
+
+def wolff_chain(N: int, K: float, C_: int, n_levels: int, seed: int, n_eq: int, n_samples: int,
+                spins: np.ndarray | None = None, trace: bool = True):
+    """The reference update rule (Wolff) + measurement: (trace, flipped, spins)."""
+    s = init_spins(N, seed) if spins is None else np.ascontiguousarray(spins, dtype=np.int8).copy()
+    tr = np.zeros((max(n_samples, 1), n_levels + 1, max(C_, 1)), dtype=np.int64) if trace else None
+    flipped = lib().orc_wolff_chain(N, K, C_, n_levels, seed, _p(s), n_eq, n_samples,
+                                    _p(tr) if trace else None)
+    if flipped < 0:
+        raise RuntimeError("orc_wolff_chain failed")
+    return (tr[:n_samples] if trace else None), int(flipped), s
+
+
+class Wolff:
+    """The reference's Wolff update (restated) with persistent state."""
+
+    def __init__(self, N: int, K: float, seed: int):
+        self.N = N
+        self.h = lib().orc_wolff_new(N, K, seed)
+        if not self.h:
+            raise MemoryError("orc_wolff_new")
+
+    def steps(self, spins: np.ndarray, n: int) -> int:
+        return int(lib().orc_wolff_steps(self.h, _p(spins), n))
+
+    def close(self):
+        if self.h:
+            lib().orc_wolff_free(self.h)
+            self.h = None
+
+
+def measure(spins: np.ndarray, C_: int, n_levels: int, seed: int, replica: int = 0, sample: int = 0):
+    s = np.ascontiguousarray(spins, dtype=np.int8)
+    out = (C.c_int64 * ((n_levels + 1) * C_))()
+    lib().orc_measure(s.shape[0], _p(s), C_, n_levels, seed, replica, sample, out)
+    return np.array(list(out), dtype=np.int64).reshape(n_levels + 1, C_)
+
+
+def exact4(K: float, C_: int = 2) -> dict:
+    n = 2 + 2 * C_ + 2 * C_ * C_
+    out = (C.c_double * n)()
+    lib().orc_exact4(K, C_, out)
+    v = list(out)
+    o = 2
+    S0 = v[o:o + C_]; o += C_
+    S1 = v[o:o + C_]; o += C_
+    S1S0 = np.array(v[o:o + C_ * C_]).reshape(C_, C_); o += C_ * C_
+    S1S1 = np.array(v[o:o + C_ * C_]).reshape(C_, C_)
+    return {"E": v[0], "M2": v[1], "S0": np.array(S0), "S1": np.array(S1), "S1S0": S1S0, "S1S1": S1S1}
+
+
+def exact4_lambda(K: float, C_: int = 2) -> float:
+    e = exact4(K, C_)
+    A = e["S1S0"] - np.outer(e["S1"], e["S0"])
+    B = e["S1S1"] - np.outer(e["S1"], e["S1"])
+    T = np.linalg.solve(B, A)
+    return float(np.max(np.linalg.eigvals(T).real))
+
+
+# ---------------------------------------------------------------------------
+# Reference harness (only where the reference sources were compiled here)
+# ---------------------------------------------------------------------------
+def ref_lib() -> C.CDLL | None:
+    global _ref
+    if _ref is None:
+        path = _build.REF_SO
+        if not os.path.exists(path):
+            if not _build.ref_available():
+                return None
+            path = _build.build_ref()
+        h = C.CDLL(path)
+        h.ref_seed.argtypes = [C.c_uint64]
+        h.ref_tie_draws.argtypes = [C.c_uint64, C.c_int, C.c_void_p]
+        h.ref_block.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_void_p]
+        h.ref_interactions.argtypes = [C.c_int, C.c_void_p, P(C.c_double)]
+        h.ref_nn_interaction.argtypes = [C.c_int, C.c_void_p]
+        h.ref_nn_interaction.restype = C.c_double
+        h.ref_energy.argtypes = [C.c_double, C.c_int, C.c_void_p]
+        h.ref_energy.restype = C.c_double
+        h.ref_trace.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p,
+                                P(C.c_double)]
+        h.ref_trace.restype = C.c_int
+        h.ref_critical_exponent.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_double, C.c_char_p,
+                                            P(C.c_double), C.c_int]
+        h.ref_critical_exponent.restype = C.c_int
+        h.ref_wolff.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_void_p]
+        _ref = h
+    return _ref
