@@ -205,6 +205,7 @@ def run_large(args, D: Dist) -> dict:
     peak, kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
     traffic = profiled_traffic("tiled_sweep_kernel")
+    tile = lat.tile_shape()
 
     # ---- end to end through the C ABI with host buffers
     hspins = torch.empty((L, L), dtype=torch.int8, pin_memory=True)
@@ -240,7 +241,7 @@ def run_large(args, D: Dist) -> dict:
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "tiled_sweep_kernel", "peak_kind": kind,
+                     "kernel": "tiled sweep_kernel", "tile": tile, "peak_kind": kind,
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(sweep_ms, 4)},
         "clocks": clocks,
         "moments_samples": tot.n_samples,
@@ -319,6 +320,13 @@ def cpu_reference(L: int, seconds: float, threads: int, n_couplings: int = 2) ->
     return {"flips_per_s": flipped / wall, "samples": samples, "wall_s": wall}
 
 
+def cpu_threads(L: int) -> int:
+    """All host threads, capped at 8 for L >= 8192 (each Wolff replica holds
+    ~2.3 GB of host state at L = 16384)."""
+    n = os.cpu_count() or 1
+    return min(n, 8) if L >= 8192 else n
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -327,7 +335,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="large", choices=["large", "batched"])
     ap.add_argument("--L", type=int, default=16384)
-    ap.add_argument("--sweeps-per-step", type=int, default=10)
+    ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--couplings", type=int, default=5)
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--batch-sweeps", type=int, default=1000)
@@ -339,7 +347,7 @@ def main():
     if args.impl == "reference":
         if D.rank != 0:
             return
-        threads = os.cpu_count() or 1
+        threads = cpu_threads(args.L)
         per = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
         vals = []
         for _ in range(args.warmup):
@@ -366,7 +374,7 @@ def main():
     else:
         out = run_batched(args, D)
     if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
+        threads = cpu_threads(args.L)
         cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads)
         out["cpu_baseline"] = {"value": round(cb["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": threads,
                                "kind": "port",

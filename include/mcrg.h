@@ -150,6 +150,10 @@ int mcrg_measure(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_
 
 /* Sweep and sample counters (the Philox time words of the next sweep / sample). */
 int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);
+/* Tile shape the autotuner picked for an HBM-tiled context (rows x bytes per
+ * colour row); MCRG_EINVAL for shared-memory-resident contexts and
+ * MCRG_EAGAIN before the first sweep.  No counterpart in the reference. */
+int mcrg_tile_shape(mcrg_ctx* ctx, int32_t* tile_rows, int32_t* tile_cols);
 /* The context's CUDA stream (cudaStream_t), for event timing. */
 int mcrg_stream(mcrg_ctx* ctx, void** stream);
 int mcrg_sync(mcrg_ctx* ctx);

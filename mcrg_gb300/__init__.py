@@ -134,6 +134,12 @@ class Lattice:
         check(lib().mcrg_counters(self._ctx, C.byref(t), C.byref(n)), "mcrg_counters")
         return int(t.value), int(n.value)
 
+    def tile_shape(self):
+        """(rows, bytes) of the autotuned sweep tile, or None for resident lattices."""
+        r, c = C.c_int32(), C.c_int32()
+        rc = lib().mcrg_tile_shape(self._ctx, C.byref(r), C.byref(c))
+        return (r.value, c.value) if rc == 0 else None
+
     def stream(self) -> int:
         s = C.c_void_p()
         check(lib().mcrg_stream(self._ctx, C.byref(s)), "mcrg_stream")

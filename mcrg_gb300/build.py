@@ -67,6 +67,29 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     return LIB
 
 
+SHIM = os.path.join(HERE, "shim")
+SHIM_BIN = os.path.join(OUT_DIR, "run_mcrg")
+
+
+def build_shim(force: bool = False) -> str:
+    """The reference-named C++ classes + the src/main.cpp-style driver,
+    linked against libmcrg.so (g++, host code only)."""
+    lib = build()
+    srcs = [os.path.join(SHIM, f) for f in ("mcrg_classes.cpp", "run_mcrg.cpp")]
+    deps = srcs + [os.path.join(SHIM, f) for f in ("mcrg_classes.hpp", "tmatrix.hpp")] + [lib]
+    if not force and os.path.exists(SHIM_BIN) and all(os.path.getmtime(d) <= os.path.getmtime(SHIM_BIN)
+                                                      for d in deps):
+        return SHIM_BIN
+    tmp = SHIM_BIN + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17"] + srcs + ["-L", OUT_DIR, "-lmcrg", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("shim build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, SHIM_BIN)
+    return SHIM_BIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
                 extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None))
+    print(build_shim(force="--force" in sys.argv))

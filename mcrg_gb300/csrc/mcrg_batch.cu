@@ -76,8 +76,6 @@ int check_request(const mcrg_request* r) {
   const int mx = ilog2i(r->L) - 1;
   const int nl = r->n_levels < 0 ? mx : r->n_levels;
   if (nl > mx) return MCRG_EINVAL;
-  if (r->L <= MCRG_SMEM_MAX_L && moment_entries(nl, r->n_couplings) > kMaxOwned * resident_threads(r->L))
-    return MCRG_EINVAL;
   return nl;
 }
 
@@ -199,7 +197,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         const ChainJob& j0 = jobs[(size_t)ranges[g].first];
         int maxlev = 0;
         for (int k = 0; k < ranges[g].second; ++k) maxlev = std::max(maxlev, jobs[(size_t)ranges[g].first + k].n_levels);
-        if (launch_chain(d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, j0.threads, ss[g]) != cudaSuccess)
+        if (launch_chain(d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads, ss[g]) != cudaSuccess)
           rc = MCRG_EIO;
         cudaEventRecord(ev[g], ss[g]);
         cudaStreamWaitEvent(s0, ev[g], 0);
@@ -375,7 +373,7 @@ void server_loop(mcrg_server* s) {
       }
       cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, sl.stream);
       cudaMemsetAsync(d_bins, 0, sizeof(mcrg_moments) * (size_t)(sl.nb > 0 ? sl.nb : 1), sl.stream);
-      launch_chain(d_job, 1, j.L, j.n_levels, j.threads, sl.stream);
+      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, sl.stream);
       if (sl.nb > 0)
         cudaMemcpyAsync(sl.h_bins, d_bins, sizeof(mcrg_moments) * (size_t)sl.nb, cudaMemcpyDeviceToHost, sl.stream);
       cudaEventRecord(sl.done, sl.stream);

@@ -158,7 +158,7 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   }
   j.bins = c->d_bins;
   CK(cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream));
-  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.threads, c->stream));
+  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.C, j.threads, c->stream));
   c->t += (uint64_t)(n_eq + n_samples * sweeps_between);
   c->n += (uint64_t)n_samples;
   *n_bins_out = nb;
@@ -228,8 +228,6 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
     return MCRG_EINVAL;
   const int nl = resolve_levels(cfg->L, cfg->n_levels);
   if (nl < 0) return MCRG_EINVAL;
-  if (cfg->L <= MCRG_SMEM_MAX_L && moment_entries(nl, cfg->n_couplings) > kMaxOwned * threads_for(cfg->L))
-    return MCRG_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) return MCRG_EIO;
   if (cudaSetDevice(cfg->device) != cudaSuccess) return MCRG_EIO;
@@ -254,7 +252,7 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
       j.key = key; j.replica = cfg->replica; j.init = 1; j.store = 1; j.bin_size = 1;
       j.state = c->d_state; j.acc = c->acc;
       if (cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
-      if (launch_chain(c->d_job, 1, j.L, nl, j.threads, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+      if (launch_chain(c->d_job, 1, j.L, nl, j.C, j.threads, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
     } else {
       c->is_tiled = true;
       rc = tiled_alloc(&c->tiled, cfg->L, nl, cfg->n_couplings, key, cfg->replica, c->acc, c->stream);
@@ -452,6 +450,15 @@ int mcrg_counters(mcrg_ctx* c, uint64_t* sweeps, uint64_t* samples) {
   if (!c) return MCRG_EINVAL;
   if (sweeps) *sweeps = c->t;
   if (samples) *samples = c->n;
+  return MCRG_OK;
+}
+
+int mcrg_tile_shape(mcrg_ctx* c, int32_t* tile_rows, int32_t* tile_cols) {
+  if (!c || !c->is_tiled) return MCRG_EINVAL;
+  int tr = 0, tc = 0;
+  if (tiled_variant(&c->tiled, &tr, &tc) < 0) return MCRG_EAGAIN;
+  if (tile_rows) *tile_rows = tr;
+  if (tile_cols) *tile_cols = tc;
   return MCRG_OK;
 }
 

@@ -20,6 +20,20 @@
 
 namespace mcrg {
 
+// One sweep of a resident lattice: colour 0, then colour 1.
+__device__ __noinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key key, uint32_t rep, const Accept& acc,
+                                         bool vec, int tid, int T) {
+  for (int c = 0; c < 2; ++c) {
+    if (vec) {
+      if (L >= 32) sweep_colour_vec<4>(lat, L, c, t, key, rep, acc, tid, T);
+      else sweep_colour_vec<2>(lat, L, c, t, key, rep, acc, tid, T);
+    } else {
+      sweep_colour_scalar(lat, L, c, t, key, rep, acc, tid, T);
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // One chain per CTA.
 // ---------------------------------------------------------------------------
@@ -31,12 +45,12 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   const Key key = J.key;
   const uint32_t rep = J.replica;
   const Accept acc = J.acc;
-  const SmemPlan plan = make_plan(L, nl);
+  const SmemPlan plan = make_plan(L, nl, C);
   uint8_t* lat = smem;
   int* S = reinterpret_cast<int*>(smem + plan.s_off);
-  int* qcount = reinterpret_cast<int*>(smem + plan.q_off);
-  uint32_t* queue = reinterpret_cast<uint32_t*>(smem + plan.q_off + 16);
-  const int qcap = plan.qcap;
+  int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
+  long long* macc = reinterpret_cast<long long*>(smem + plan.acc_off);
+  const int E = plan.E;
   const bool vec = acc.fast && L >= 16;
 
   // ---- configuration into shared memory
@@ -47,59 +61,35 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
     uint4* dst = reinterpret_cast<uint4*>(lat);
     for (int v = tid; v < L * L / 16; v += T) dst[v] = src[v];
   }
-  if (tid < 2) qcount[tid] = 0;
-
-  // ---- moment entries owned by this thread
-  const int E = (nl + 1) * C + 2 * nl * C * C;
-  int16_t ox[kMaxOwned], oy[kMaxOwned];
-  int oidx[kMaxOwned];
-  int64_t oacc[kMaxOwned];
-#pragma unroll
-  for (int r = 0; r < kMaxOwned; ++r) {
-    const int e = tid + r * T;
-    oacc[r] = 0;
-    ox[r] = -1; oy[r] = -1; oidx[r] = -1;
+  // ---- moment entries: x | y << 16 (indices into S, y = 0xFFFF for a plain sum)
+  //      and the output slot (kind << 16 | index into S / SbS / SbSb)
+  for (int e = tid; e < E; e += T) {
+    int x, y, out;
     if (e < (nl + 1) * C) {
       const int l = e / C, c = e % C;
-      ox[r] = (int16_t)(l * MCRG_MAX_COUPLINGS + c);
-      oidx[r] = l * MCRG_MAX_COUPLINGS + c;
-    } else if (e < E) {
+      x = l * MCRG_MAX_COUPLINGS + c;
+      y = 0xFFFF;
+      out = x;
+    } else {
       const int e2 = e - (nl + 1) * C, kind = e2 / (nl * C * C), e3 = e2 % (nl * C * C);
       const int l = e3 / (C * C), a = (e3 % (C * C)) / C, b = e3 % C;
-      ox[r] = (int16_t)((l + 1) * MCRG_MAX_COUPLINGS + a);
-      oy[r] = (int16_t)((kind == 0 ? l : l + 1) * MCRG_MAX_COUPLINGS + b);
-      oidx[r] = (1 + kind) * 100000 + (l * MCRG_MAX_COUPLINGS + a) * MCRG_MAX_COUPLINGS + b;
+      x = (l + 1) * MCRG_MAX_COUPLINGS + a;
+      y = (kind == 0 ? l : l + 1) * MCRG_MAX_COUPLINGS + b;
+      out = ((1 + kind) << 16) | ((l * MCRG_MAX_COUPLINGS + a) * MCRG_MAX_COUPLINGS + b);
     }
+    tab[e] = make_int2(x | (y << 16), out);
+    macc[e] = 0;
   }
-  sync_group();
+  __syncthreads();
 
   uint32_t t = J.t0;
-  auto sweep = [&](uint32_t tt) {
-    for (int c = 0; c < 2; ++c) {
-      if (vec) {
-        if (L >= 32) sweep_colour_vec<4>(lat, L, c, tt, key, rep, acc, &qcount[c], queue, qcap, tid, T);
-        else sweep_colour_vec<2>(lat, L, c, tt, key, rep, acc, &qcount[c], queue, qcap, tid, T);
-        sync_group();
-        const int cnt = qcount[c];
-        if (cnt) resolve_queue(lat, L, c, tt, key, rep, acc, cnt, queue, qcap, tid, T);
-        sync_group();
-        if (tid == 0) qcount[c] = 0;
-      } else {
-        sweep_colour_scalar(lat, L, c, tt, key, rep, acc, tid, T);
-        sync_group();
-      }
-    }
-  };
-
-  for (int64_t s = 0; s < J.n_eq; ++s) sweep(t++);
-
-  int64_t in_bin = 0, bin = 0;
+  for (int64_t s = 0; s < J.n_eq; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T);
   for (int64_t n = 0; n < J.n_samples; ++n) {
-    for (int64_t s = 0; s < J.sweeps_between; ++s) sweep(t++);
-    // ---- measurement: every level's coupling sums, blocking level by level
+    for (int64_t s = 0; s < J.sweeps_between; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T);
+    // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
-    sync_group();
+    __syncthreads();
     int m = L;
     for (int l = 0; l <= nl; ++l, m >>= 1) {
       const uint8_t* lev = smem + plan.off[l];
@@ -113,42 +103,40 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
         if (m >= 32) block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
         else block_scalar(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
       }
-      sync_group();
+      __syncthreads();
     }
-    // ---- moments
-#pragma unroll
-    for (int r = 0; r < kMaxOwned; ++r) {
-      if (ox[r] >= 0) {
-        const int64_t x = S[ox[r]];
-        oacc[r] += oy[r] >= 0 ? x * (int64_t)S[oy[r]] : x;
-      }
+    // ---- moment products (each entry owned by one thread)
+    for (int e = tid; e < E; e += T) {
+      const int2 te = tab[e];
+      const long long xv = S[te.x & 0xFFFF];
+      const int yi = (te.x >> 16) & 0xFFFF;
+      macc[e] += yi == 0xFFFF ? xv : xv * (long long)S[yi];
     }
-    ++in_bin;
-    if (in_bin == J.bin_size || n == J.n_samples - 1) {
-      mcrg_moments* out = J.bins + bin;
-#pragma unroll
-      for (int r = 0; r < kMaxOwned; ++r) {
-        if (oidx[r] < 0) continue;
-        if (oidx[r] < 100000) {
-          out->S[oidx[r]] = oacc[r];
+    // ---- bin boundary: flush and restart the sums
+    const bool last = n == J.n_samples - 1;
+    if ((n + 1) % J.bin_size == 0 || last) {
+      mcrg_moments* out = J.bins + n / J.bin_size;
+      for (int e = tid; e < E; e += T) {
+        const int o = tab[e].y, kind = o >> 16, idx = o & 0xFFFF;
+        const long long v = macc[e];
+        if (kind == 0) {
+          out->S[idx] = v;
         } else {
-          mcrg_i128 v;
-          v.lo = (uint64_t)oacc[r];
-          v.hi = oacc[r] >> 63;
-          if (oidx[r] < 200000) out->SbS[oidx[r] - 100000] = v;
-          else out->SbSb[oidx[r] - 200000] = v;
+          mcrg_i128 w;
+          w.lo = (uint64_t)v;
+          w.hi = v >> 63;
+          if (kind == 1) out->SbS[idx] = w;
+          else out->SbSb[idx] = w;
         }
-        oacc[r] = 0;
+        macc[e] = 0;
       }
       if (tid == 0) {
         out->n_levels = nl;
         out->n_couplings = C;
-        out->n_samples = in_bin;
+        out->n_samples = last ? (n % J.bin_size) + 1 : J.bin_size;
       }
-      in_bin = 0;
-      ++bin;
     }
-    sync_group();
+    __syncthreads();
   }
 
   // ---- final configuration back to HBM
@@ -179,9 +167,9 @@ __global__ void couplings_once_kernel(const uint8_t* in, int N, int C, int* out)
   reduce_into(a5, out, C);
 }
 
-cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int threads,
+cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads,
                          cudaStream_t stream) {
-  const SmemPlan plan = make_plan(L, n_levels);
+  const SmemPlan plan = make_plan(L, n_levels, C);
   static int configured = 0;
   if (plan.bytes > configured) {
     cudaError_t e = cudaFuncSetAttribute(chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

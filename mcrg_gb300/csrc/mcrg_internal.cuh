@@ -24,16 +24,18 @@ struct ChainJob {
   Accept acc;
 };
 
-// Shared-memory plan of a resident lattice and its blocked levels.
+// Shared-memory plan of a resident lattice, its blocked levels and (when
+// C > 0) the moment accumulators of one chain.
 struct SmemPlan {
   int off[MCRG_MAX_LEVELS + 2];
   int s_off;    // int32 S[(MCRG_MAX_LEVELS+1) * MCRG_MAX_COUPLINGS]
-  int q_off;    // int32 qcount[2], then uint32 queue[qcap]
-  int qcap;
+  int tab_off;  // int2 per moment entry: (x | y << 16, output index)
+  int acc_off;  // int64 per moment entry
+  int E;        // moment entries
   int bytes;
 };
 
-__host__ __device__ inline SmemPlan make_plan(int L, int n_levels) {
+__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
   SmemPlan p;
   int off = 0, n = L;
   for (int l = 0; l <= n_levels; ++l, n >>= 1) {
@@ -42,25 +44,23 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels) {
   }
   p.s_off = off;
   off += ((MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS * 4 + 15) / 16 * 16;
-  p.q_off = off;
-  int qcap = (L * L) / 64;
-  if (qcap < 64) qcap = 64;
-  p.qcap = qcap;
-  off += 16 + qcap * 4;
+  p.E = C > 0 ? (n_levels + 1) * C + 2 * n_levels * C * C : 0;
+  p.tab_off = off;
+  off += ((p.E * 8 + 15) / 16) * 16;
+  p.acc_off = off;
+  off += p.E * 8;
   p.bytes = (off + 15) / 16 * 16;
   return p;
 }
-
-// Largest number of moment entries one thread owns in the chain kernel.
-constexpr int kMaxOwned = 8;
 
 inline int moment_entries(int n_levels, int C) { return (n_levels + 1) * C + 2 * n_levels * C * C; }
 
 // Host: acceptance parameters for coupling K (FP64, see include/mcrg.h).
 Accept make_accept(double K);
 
-// Launch `n_jobs` chains (all with the same L, n_levels and threads).
-cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int threads,
+// Launch `n_jobs` chains (all with the same L and threads; n_levels and C
+// bound the shared memory of every job).
+cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads,
                          cudaStream_t stream);
 
 // Stateless helpers on a device lattice in split layout (used by

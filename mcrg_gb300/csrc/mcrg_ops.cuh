@@ -29,18 +29,6 @@ __device__ __forceinline__ void store_words(uint8_t* p, const uint32_t (&w)[NW])
 }
 __device__ __forceinline__ uint32_t load_word(const uint8_t* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
-// Tie entry: row << 14 | k << 1 | m (m in {0,1}); row < 2^18, k < 8192.
-__device__ __forceinline__ uint32_t tie_entry(int i, int k, uint32_t m) {
-  return ((uint32_t)i << 14) | ((uint32_t)k << 1) | (m & 1u);
-}
-
-__device__ __forceinline__ bool resolve_tie(Key key, uint32_t replica, int c, int i, int k, uint32_t m,
-                                            uint32_t t, const Accept& a) {
-  const uint4 lo = stream_block(key, replica, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
-  const uint32_t r24 = u4get(lo, k & 3) & 0xFFFFFFu;
-  return r24 < (a.thr[m] & 0xFFFFFFu);
-}
-
 // ---------------------------------------------------------------------------
 // Initial coin (P_INIT): spin bit of (colour c, row i, k) = bit (k&127) of
 // the block (row i, group k>>7, sub c, time 0).
@@ -66,94 +54,100 @@ __device__ void init_level0(uint8_t* lat, int L, Key key, uint32_t rep, int tid,
 }
 
 // ---------------------------------------------------------------------------
-// SWAR update of one chunk of NW words of colour c.  tw: the chunk; uw/dw:
-// the other colour's chunks in the rows above / below; mw: the other colour's
-// chunk in the same row; e: the byte just past the chunk (q = 1) or just
-// before it (q = 0) in that row; R: the chunk's P_SWEEP_HI block.  Writes
-// the updated words to nw and the open (tied) bytes to ties; returns their OR.
+// SWAR update of one chunk of NW words (4*NW sites) of colour c.  tw: the
+// chunk (updated in place); uw / dw: the other colour's chunks in the rows
+// above / below; mw: the other colour's chunk in the same row; prv / nxt: the
+// aligned words just before / after mw in that row (only their top / low byte
+// is used); q: the side neighbour is O[i][k+1] when q = 1, O[i][k-1] when
+// q = 0; R: the chunk's P_SWEEP_HI block.  Returns the still-open sites as
+// a mask with bit (8*b + 7 - j) for byte b of word j.
 // ---------------------------------------------------------------------------
 template <int NW>
-__device__ __forceinline__ uint32_t chunk_update(const uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
-                                                 const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t e,
-                                                 uint32_t q, const uint4& R, const Accept& a, uint32_t (&nw)[NW],
-                                                 uint32_t (&ties)[NW]) {
-  uint32_t tie_any = 0;
+__device__ __forceinline__ uint32_t update_chunk(uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
+                                                 const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t prv,
+                                                 uint32_t nxt, uint32_t q, const uint4& R, const Accept& a) {
+  uint32_t V[NW + 1];
+  V[0] = q ? mw[0] : prv;
+#pragma unroll
+  for (int j = 1; j < NW; ++j) V[j] = q ? mw[j] : mw[j - 1];
+  V[NW] = q ? nxt : mw[NW - 1];
+  const uint32_t sh = 24u - 16u * q;
+  uint32_t open = 0;
 #pragma unroll
   for (int j = 0; j < NW; ++j) {
-    // side neighbour: O[i][k+1] when q = 1, O[i][k-1] when q = 0
-    const uint32_t nxt = (j + 1 < NW) ? mw[j + 1] : e;
-    const uint32_t prv = (j > 0) ? mw[j - 1] : (e << 24);
-    const uint32_t side = q ? __funnelshift_r(mw[j], nxt, 8) : __funnelshift_r(prv, mw[j], 24);
-    nw[j] = swar_update(tw[j], uw[j], dw[j], mw[j], side, u4get(R, j), a, &ties[j]);
-    tie_any |= ties[j];
+    uint32_t tie;
+    const uint32_t side = __funnelshift_r(V[j], V[j + 1], sh);
+    tw[j] = swar_update(tw[j], uw[j], dw[j], mw[j], side, u4get(R, j), a, &tie);
+    open |= tie >> j;
   }
-  return tie_any;
+  return open;
 }
 
-// Queues (or, when the queue is full, resolves in place) the open sites of
-// a chunk.  ent(k) gives the queue entry of chunk byte k (k = 4j + byte);
-// resolve(k, m) gives the exact decision for that byte.
-template <int NW, class Ent, class Res>
-__device__ __forceinline__ void queue_ties(const uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
-                                           const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t e,
-                                           uint32_t q, const uint32_t (&ties)[NW], uint32_t (&nw)[NW],
-                                           int* qcount, uint32_t* queue, int qcap, Ent ent, Res resolve) {
-#pragma unroll
-  for (int j = 0; j < NW; ++j) {
-    uint32_t tb = ties[j];
-    while (tb) {
-      const int byte = (__ffs(tb) - 1) >> 3;
-      tb &= tb - 1;
-      const uint32_t nxt = (j + 1 < NW) ? mw[j + 1] : e;
-      const uint32_t prv = (j > 0) ? mw[j - 1] : (e << 24);
-      const uint32_t side = q ? __funnelshift_r(mw[j], nxt, 8) : __funnelshift_r(prv, mw[j], 24);
-      const uint32_t m = (swar_m(tw[j], uw[j], dw[j], mw[j], side) >> (8 * byte)) & 0xFFu;
-      const int slot = atomicAdd(qcount, 1);
-      if (slot < qcap) queue[slot] = ent(4 * j + byte, m);
-      else if (resolve(4 * j + byte, m)) nw[j] ^= 1u << (8 * byte);
-    }
-  }
+// Chunk byte of bit p of an open-site mask.
+__device__ __forceinline__ int open_byte(int p) { return 4 * (7 - (p & 7)) + (p >> 3); }
+
+// Exact decision for an open site (top byte of its draw equal to the top
+// byte of its threshold): flip iff the low 24 bits of the P_SWEEP_LO draw
+// are below the threshold's.  t: the site; n0..n3: its neighbours.
+__device__ __forceinline__ bool resolve_open(uint32_t t, uint32_t n0, uint32_t n1, uint32_t n2, uint32_t n3,
+                                             Key key, uint32_t rep, uint32_t c, int i, int k, uint32_t tt,
+                                             const Accept& a) {
+  const uint32_t m = (n0 != t) + (n1 != t) + (n2 != t) + (n3 != t);
+  if (m > 1) return false;  // only reachable for unused halo bytes of a staged tile
+  const uint4 lo = stream_block(key, rep, P_SWEEP_LO, c, (uint32_t)i, (uint32_t)(k >> 2), tt);
+  return (u4get(lo, k & 3) & 0xFFFFFFu) < (a.thr[m] & 0xFFFFFFu);
 }
 
-// Vector sweep of colour c on an n x n resident lattice (n >= 16).
+// Vector sweep of colour c of a resident n x n lattice (n >= 16).  Threads
+// take chunks in rounds of up to 8, keep the open-site masks in registers and
+// resolve their own open sites at the end of each round.
 template <int NW>
 __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
-                                 const Accept& a, int* qcount, uint32_t* queue, int qcap, int tid, int T) {
+                                 const Accept& a, int tid, int T) {
   constexpr int CB = 4 * NW;  // chunk bytes
-  const int half = n / 2, cpr = half / CB;
+  const int half = n / 2, cpr = half / CB, ntask = n * cpr;
   uint8_t* Cc = lat + (size_t)c * n * half;
   const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
-  for (int task = tid; task < n * cpr; task += T) {
-    const int i = task / cpr, k0 = (task % cpr) * CB;
-    const uint32_t q = (uint32_t)((i + c) & 1);
-    uint8_t* tp = Cc + (size_t)i * half + k0;
-    uint32_t tw[NW], uw[NW], dw[NW], mw[NW];
-    load_words<NW>(tp, tw);
-    load_words<NW>(Oc + (size_t)((i - 1) & (n - 1)) * half + k0, uw);
-    load_words<NW>(Oc + (size_t)((i + 1) & (n - 1)) * half + k0, dw);
-    load_words<NW>(Oc + (size_t)i * half + k0, mw);
-    const uint32_t e = Oc[(size_t)i * half + ((q ? (k0 + CB) : (k0 - 1)) & (half - 1))];
-    const uint4 R = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 4), t);
-    uint32_t nw[NW], ties[NW];
-    if (chunk_update<NW>(tw, uw, dw, mw, e, q, R, a, nw, ties)) {
-      queue_ties<NW>(tw, uw, dw, mw, e, q, ties, nw, qcount, queue, qcap,
-                     [&](int kb, uint32_t m) { return tie_entry(i, k0 + kb, m); },
-                     [&](int kb, uint32_t m) { return resolve_tie(key, rep, c, i, k0 + kb, m, t, a); });
+  for (int base = 0; base < ntask; base += 8 * T) {
+    uint32_t om[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int task = base + tid + r * T;
+      om[r] = 0;
+      if (task < ntask) {
+        const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB;
+        const uint32_t q = (uint32_t)((i + c) & 1);
+        uint8_t* tp = Cc + (size_t)i * half + k0;
+        const uint8_t* orow = Oc + (size_t)i * half;
+        uint32_t tw[NW], uw[NW], dw[NW], mw[NW];
+        load_words<NW>(tp, tw);
+        load_words<NW>(Oc + (size_t)((i - 1) & (n - 1)) * half + k0, uw);
+        load_words<NW>(Oc + (size_t)((i + 1) & (n - 1)) * half + k0, dw);
+        load_words<NW>(orow + k0, mw);
+        const uint32_t prv = load_word(orow + ((k0 - 4) & (half - 1)));
+        const uint32_t nxt = load_word(orow + ((k0 + CB) & (half - 1)));
+        const uint4 R = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 4), t);
+        om[r] = update_chunk<NW>(tw, uw, dw, mw, prv, nxt, q, R, a);
+        store_words<NW>(tp, tw);
+      }
     }
-    store_words<NW>(tp, nw);
-  }
-}
-
-__device__ void resolve_queue(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep, const Accept& a,
-                              int count, const uint32_t* queue, int qcap, int tid, int T) {
-  const int half = n / 2;
-  uint8_t* Cc = lat + (size_t)c * n * half;
-  const int cnt = count < qcap ? count : qcap;
-  for (int e = tid; e < cnt; e += T) {
-    const uint32_t v = queue[e];
-    const int i = (int)(v >> 14), k = (int)((v >> 1) & 0x1FFFu);
-    const uint32_t m = v & 1u;
-    if (resolve_tie(key, rep, c, i, k, m, t, a)) Cc[(size_t)i * half + k] ^= 1u;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      uint32_t bits = om[r];
+      if (!bits) continue;
+      const int task = base + tid + r * T;
+      const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB, q = (i + c) & 1;
+      while (bits) {
+        const int p = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int k = k0 + open_byte(p);
+        uint8_t* sp = Cc + (size_t)i * half + k;
+        const uint8_t* orow = Oc + (size_t)i * half;
+        if (resolve_open(*sp, Oc[(size_t)((i - 1) & (n - 1)) * half + k], Oc[(size_t)((i + 1) & (n - 1)) * half + k],
+                         orow[(k - 1 + q) & (half - 1)], orow[(k + q) & (half - 1)], key, rep, (uint32_t)c, i, k, t, a))
+          *sp ^= 1u;
+      }
+    }
   }
 }
 

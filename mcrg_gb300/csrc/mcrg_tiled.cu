@@ -19,205 +19,19 @@
 // exactly in int128 (per-sample products of the level-0 sums reach 2^60).
 #include <cstring>
 
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "mcrg_ops.cuh"
+#include "mcrg_sweep_tiled.cuh"
 #include "mcrg_tiled.cuh"
 
 namespace mcrg {
 
 namespace {
-
-struct TileParams {
-  int L, h, TR, TC, pitch, tiles_x, n_tiles, qcap;
-  Key key;
-  uint32_t rep;
-  Accept acc;
-};
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-// Copies global bytes [k - 16, k - 16 + len) (mod h) of one row into dst.
-__device__ __forceinline__ void stage_row(uint8_t* dst, const uint8_t* row, int h, int k0, int len, uint64_t* bar) {
-  int g = k0 - 16;
-  if (g < 0) g += h;
-  int z = 0;
-  while (z < len) {
-    const int run = min(len - z, h - g);
-    bulk_g2s(dst + z, row + g, (uint32_t)run, bar);
-    z += run;
-    g = 0;
-  }
-}
-
-constexpr uint32_t kWaitLimit = 1u << 24;
-
-__global__ void __launch_bounds__(256, 2)
-    tiled_sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, TileParams P, uint32_t t,
-                       int* __restrict__ status) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-  int* qcount = reinterpret_cast<int*>(smem + 16);
-  uint32_t* queue = reinterpret_cast<uint32_t*>(smem + 32);
-  uint8_t* Ws = smem + 32 + ((P.qcap * 4 + 127) / 128) * 128;
-  uint8_t* Bs = Ws + (size_t)(P.TR + 4) * P.pitch;
-  const int tid = threadIdx.x, T = blockDim.x;
-  const int L = P.L, h = P.h, TR = P.TR, TC = P.TC, pitch = P.pitch;
-  const size_t plane = (size_t)L * h;
-  const Accept a = P.acc;
-  const Key key = P.key;
-  const uint32_t rep = P.rep;
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  if (tid < 4) qcount[tid] = 0;
-  __syncthreads();
-  uint32_t phase = 0;
-  const int rows_staged = 2 * TR + 6;
-  const int cpr_all = pitch / 16;  // chunks per staged row (tile + both halos)
-  for (int tile = blockIdx.x; tile < P.n_tiles; tile += gridDim.x) {
-    const int r0 = (tile / P.tiles_x) * TR, k0 = (tile % P.tiles_x) * TC;
-    // ---- stage the tile (one warp issues the bulk copies)
-    if (tid < 32) {
-      if (tid == 0) {
-        fence_proxy_async();
-        mbar_expect_tx(bar, (uint32_t)(rows_staged * pitch));
-      }
-      __syncwarp();
-      for (int r = tid; r < rows_staged; r += 32) {
-        if (r < TR + 4) {
-          const int g = (r0 - 2 + r + L) & (L - 1);
-          stage_row(Ws + (size_t)r * pitch, in + plane + (size_t)g * h, h, k0, pitch, bar);
-        } else {
-          const int rr = r - (TR + 4);
-          const int g = (r0 - 1 + rr + L) & (L - 1);
-          stage_row(Bs + (size_t)rr * pitch, in + (size_t)g * h, h, k0, pitch, bar);
-        }
-      }
-    }
-    bool ok = false;
-    for (uint32_t it = 0; it < kWaitLimit && !ok; ++it) ok = mbar_try_wait(bar, phase);
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(status, 1);
-      return;
-    }
-    phase ^= 1u;
-
-    // ---- colour 0 on rows r0-1 .. r0+TR (tile + halo), all staged columns
-    for (int task = tid; task < (TR + 2) * cpr_all; task += T) {
-      const int y = task / cpr_all, z0 = (task % cpr_all) * 16;
-      const int gr = (r0 - 1 + y + L) & (L - 1);
-      const uint32_t q = (uint32_t)(gr & 1);
-      int gk = k0 - 16 + z0;
-      if (gk < 0) gk += h;
-      if (gk >= h) gk -= h;
-      uint8_t* tp = Bs + (size_t)y * pitch + z0;
-      const uint8_t* mid = Ws + (size_t)(y + 1) * pitch;
-      uint32_t tw[4], uw[4], dw[4], mw[4], nw[4], ties[4];
-      load_words4(tp, tw);
-      load_words4(Ws + (size_t)y * pitch + z0, uw);
-      load_words4(Ws + (size_t)(y + 2) * pitch + z0, dw);
-      load_words4(mid + z0, mw);
-      uint32_t e = 0;
-      if (q) { if (z0 + 16 < pitch) e = mid[z0 + 16]; }
-      else if (z0 > 0) e = mid[z0 - 1];
-      const uint4 R = stream_block(key, rep, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(gk >> 4), t);
-      if (chunk_update<4>(tw, uw, dw, mw, e, q, R, a, nw, ties)) {
-        queue_ties<4>(tw, uw, dw, mw, e, q, ties, nw, &qcount[0], queue, P.qcap,
-                      [&](int kb, uint32_t m) { return tie_entry(y, z0 + kb, m); },
-                      [&](int kb, uint32_t m) { return resolve_tie(key, rep, 0, gr, gk + kb, m, t, a); });
-      }
-      store_words<4>(tp, nw);
-    }
-    __syncthreads();
-    {
-      const int cnt = min(qcount[0], P.qcap);
-      for (int x = tid; x < cnt; x += T) {
-        const uint32_t v = queue[x];
-        const int y = (int)(v >> 14), z = (int)((v >> 1) & 0x1FFFu);
-        const uint32_t m = v & 1u;
-        const int gr = (r0 - 1 + y + L) & (L - 1);
-        int gk = k0 - 16 + z;
-        if (gk < 0) gk += h;
-        if (gk >= h) gk -= h;
-        if (resolve_tie(key, rep, 0, gr, gk, m, t, a)) Bs[(size_t)y * pitch + z] ^= 1u;
-      }
-    }
-    __syncthreads();
-    if (tid == 0) qcount[0] = 0;
-
-    // ---- colour 1 on the tile rows r0 .. r0+TR-1, tile columns
-    const int cpr_in = TC / 16;
-    for (int task = tid; task < TR * cpr_in; task += T) {
-      const int x = 2 + task / cpr_in, z0 = 16 + (task % cpr_in) * 16;
-      const int gr = r0 + x - 2;
-      const uint32_t q = (uint32_t)((gr + 1) & 1);
-      const int gk = k0 - 16 + z0;
-      uint8_t* tp = Ws + (size_t)x * pitch + z0;
-      const uint8_t* mid = Bs + (size_t)(x - 1) * pitch;
-      uint32_t tw[4], uw[4], dw[4], mw[4], nw[4], ties[4];
-      load_words4(tp, tw);
-      load_words4(Bs + (size_t)(x - 2) * pitch + z0, uw);
-      load_words4(Bs + (size_t)x * pitch + z0, dw);
-      load_words4(mid + z0, mw);
-      const uint32_t e = q ? mid[z0 + 16] : mid[z0 - 1];
-      const uint4 R = stream_block(key, rep, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(gk >> 4), t);
-      if (chunk_update<4>(tw, uw, dw, mw, e, q, R, a, nw, ties)) {
-        queue_ties<4>(tw, uw, dw, mw, e, q, ties, nw, &qcount[1], queue, P.qcap,
-                      [&](int kb, uint32_t m) { return tie_entry(x, z0 + kb, m); },
-                      [&](int kb, uint32_t m) { return resolve_tie(key, rep, 1, gr, gk + kb, m, t, a); });
-      }
-      store_words<4>(tp, nw);
-    }
-    __syncthreads();
-    {
-      const int cnt = min(qcount[1], P.qcap);
-      for (int xx = tid; xx < cnt; xx += T) {
-        const uint32_t v = queue[xx];
-        const int x = (int)(v >> 14), z = (int)((v >> 1) & 0x1FFFu);
-        const uint32_t m = v & 1u;
-        if (resolve_tie(key, rep, 1, r0 + x - 2, k0 - 16 + z, m, t, a)) Ws[(size_t)x * pitch + z] ^= 1u;
-      }
-    }
-    __syncthreads();
-    if (tid == 0) qcount[1] = 0;
-
-    // ---- write the tile (both colours) to the output buffer
-    for (int task = tid; task < 2 * TR * cpr_in; task += T) {
-      const int c = task / (TR * cpr_in), rem = task % (TR * cpr_in);
-      const int rr = rem / cpr_in, z0 = 16 + (rem % cpr_in) * 16;
-      const uint8_t* src = c == 0 ? Bs + (size_t)(rr + 1) * pitch + z0 : Ws + (size_t)(rr + 2) * pitch + z0;
-      uint8_t* dst = out + (size_t)c * plane + (size_t)(r0 + rr) * h + (k0 - 16 + z0);
-      *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(src);
-    }
-    __syncthreads();
-  }
-}
 
 __global__ void tiled_init_kernel(uint8_t* lat, int L, Key key, uint32_t rep) {
   init_level0(lat, L, key, rep, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
@@ -322,25 +136,49 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
 
 int g_num_sms = 0;
 
-TileParams tile_params(const TiledLattice* t) {
-  TileParams P;
+// Tile-shape variants of the fused sweep; the autotuner picks one per
+// (L, device) by timing each eligible variant on the live lattice.
+struct Variant {
+  int TR, TC;
+  void (*kern)(const uint8_t*, uint8_t*, tiled::Params, uint32_t, int*);
+  size_t smem;
+};
+
+#define MCRG_VARIANT(TR_, TC_) \
+  Variant { TR_, TC_, tiled::sweep_kernel<TR_, TC_, 256>, tiled::sweep_smem_bytes<TR_, TC_>() }
+
+const Variant kVariants[] = {MCRG_VARIANT(32, 1024), MCRG_VARIANT(16, 1024), MCRG_VARIANT(32, 512),
+                             MCRG_VARIANT(64, 512),  MCRG_VARIANT(16, 512),  MCRG_VARIANT(32, 256),
+                             MCRG_VARIANT(16, 2048)};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+bool variant_fits(const Variant& v, int L) { return (L / 2) % v.TC == 0 && L % v.TR == 0; }
+
+tiled::Params params_for(const TiledLattice* t, const Variant& v) {
+  tiled::Params P;
   memset(&P, 0, sizeof P);
   P.L = t->L;
   P.h = t->L / 2;
-  P.TR = t->tile_rows;
-  P.TC = t->tile_cols;
-  P.pitch = P.TC + 32;
-  P.tiles_x = P.h / P.TC;
-  P.n_tiles = (P.L / P.TR) * P.tiles_x;
-  P.qcap = 1024;
+  P.tiles_x = P.h / v.TC;
+  P.n_tiles = (P.L / v.TR) * P.tiles_x;
   P.key = t->key;
   P.rep = t->replica;
   P.acc = t->acc;
   return P;
 }
 
-size_t sweep_smem(const TileParams& P) {
-  return 32 + (size_t)((P.qcap * 4 + 127) / 128) * 128 + (size_t)(2 * P.TR + 6) * P.pitch;
+int ctas_for(const Variant& v, int n_tiles) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, 256, v.smem);
+  if (per_sm < 1) per_sm = 1;
+  int c = g_num_sms * per_sm;
+  return c < n_tiles ? c : n_tiles;
+}
+
+void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
+  const Variant& v = kVariants[vi];
+  const tiled::Params P = params_for(t, v);
+  v.kern<<<ctas_for(v, P.n_tiles), 256, v.smem, s>>>(in, out, P, tt, t->d_status);
 }
 
 int first_tail_level(int L) {
@@ -359,8 +197,6 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
   t->key = key;
   t->replica = replica;
   t->acc = acc;
-  t->tile_rows = 32;
-  t->tile_cols = (L / 2) < 1024 ? (L / 2) : 1024;
   if (!acc.fast) return MCRG_ENOSYS;  // the tiled sweep implements the K < -ln2/4 fast path only
   if (g_num_sms == 0) {
     int dev = 0;
@@ -384,16 +220,12 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
   if (cudaMalloc(&t->d_status, sizeof(int)) != cudaSuccess) return MCRG_ENOMEM;
   cudaMemsetAsync(t->d_S, 0, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS, s);
   cudaMemsetAsync(t->d_status, 0, sizeof(int), s);
-  const TileParams P = tile_params(t);
-  if (cudaFuncSetAttribute(tiled_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem(P)) !=
-      cudaSuccess)
-    return MCRG_EIO;
+  for (int v = 0; v < kNumVariants; ++v)
+    if (cudaFuncSetAttribute(kVariants[v].kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kVariants[v].smem) != cudaSuccess)
+      return MCRG_EIO;
   cudaFuncSetAttribute(tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tiled_sweep_kernel, 256, sweep_smem(P));
-  if (per_sm < 1) per_sm = 1;
-  t->ctas = g_num_sms * per_sm;
-  if (t->ctas > P.n_tiles) t->ctas = P.n_tiles;
+  t->variant = -1;
   tiled_init_kernel<<<g_num_sms * 8, 256, 0, s>>>(t->buf[0], L, key, replica);
   t->cur = 0;
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
@@ -412,12 +244,68 @@ void tiled_free(TiledLattice* t) {
 uint8_t* tiled_state(TiledLattice* t) { return t->buf[t->cur]; }
 mcrg_moments* tiled_bins(TiledLattice* t) { return t->d_bins; }
 
+// Picks the fastest eligible tile shape for this lattice side on this device
+// (MCRG_TILE=<TR>x<TC> forces one).  Each candidate runs a few sweeps that
+// write the idle ping-pong buffer only, so the chain state does not move.
+static int autotune(TiledLattice* t, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (const char* force = getenv("MCRG_TILE")) {
+    int tr = 0, tc = 0;
+    if (sscanf(force, "%dx%d", &tr, &tc) == 2)
+      for (int v = 0; v < kNumVariants; ++v)
+        if (kVariants[v].TR == tr && kVariants[v].TC == tc && variant_fits(kVariants[v], t->L)) return v;
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({t->L, dev});
+    if (it != cache.end()) return it->second;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = -1;
+  float best_ms = 1e30f;
+  const int reps = t->L >= 4096 ? 3 : 10;
+  for (int v = 0; v < kNumVariants; ++v) {
+    if (!variant_fits(kVariants[v], t->L)) continue;
+    launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u, s);  // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps; ++r) launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u + r, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best < 0) return -1;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[{t->L, dev}] = best;
+  return best;
+}
+
+int tiled_variant(TiledLattice* t, int* TR, int* TC) {
+  if (t->variant < 0) return -1;
+  if (TR) *TR = kVariants[t->variant].TR;
+  if (TC) *TC = kVariants[t->variant].TC;
+  return t->variant;
+}
+
 int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s) {
-  const TileParams P = tile_params(t);
-  const size_t sm = sweep_smem(P);
+  if (n <= 0) return MCRG_OK;
+  if (t->variant < 0) {
+    t->variant = autotune(t, s);
+    if (t->variant < 0) return MCRG_ENOSYS;
+  }
   for (int64_t k = 0; k < n; ++k) {
-    tiled_sweep_kernel<<<t->ctas, 256, sm, s>>>(t->buf[t->cur], t->buf[t->cur ^ 1], P, t0 + (uint32_t)k,
-                                                t->d_status);
+    launch_variant(t, t->variant, t->buf[t->cur], t->buf[t->cur ^ 1], t0 + (uint32_t)k, s);
     t->cur ^= 1;
   }
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;

@@ -1,0 +1,120 @@
+// mcrg_classes.hpp -- the reference's host classes over the libmcrg C ABI.
+//
+// Same names, signatures and argument meaning as kim-jane/MCRG's
+//   Lattice                          (src/lattice.hpp:5-37)
+//   IsingModel                       (src/ising.hpp:8-41)
+//   MonteCarloRenormalizationGroup   (src/mcrg.hpp:6-40)
+// so src/main.cpp's call sites compile against this header.  Differences a
+// caller can observe:
+//   - the lattice lives on the GPU; spins_ is a host mirror refreshed after
+//     every device operation (set mirror_spins_ = false to skip the copy);
+//   - sample_new_configuration() is one checkerboard Metropolis sweep, not a
+//     Wolff cluster step (same stationary distribution);
+//   - the RG eigen-solve is a small FP64 routine (tmatrix.hpp) instead of
+//     Eigen, applied to exact integer moment sums;
+//   - errors from the device surface as McrgError exceptions on the C++ side
+//     (the reference has no error reporting).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mcrg.h"
+
+class McrgError : public std::runtime_error {
+ public:
+  McrgError(int code, const std::string& what)
+      : std::runtime_error(what + ": " + mcrg_strerror(code)), code_(code) {}
+  int code() const { return code_; }
+
+ private:
+  int code_;
+};
+
+// Minimal stand-in for the reference's `imat` (Eigen column-major int
+// matrix): spins_(i, j) indexing, rows(), cols(), sum().
+class SpinMatrix {
+ public:
+  SpinMatrix() = default;
+  SpinMatrix(int n, int m) : n_(n), m_(m), d_((size_t)n * m, 0) {}
+  int& operator()(int i, int j) { return d_[(size_t)j * n_ + i]; }
+  int operator()(int i, int j) const { return d_[(size_t)j * n_ + i]; }
+  int rows() const { return n_; }
+  int cols() const { return m_; }
+  long long sum() const {
+    long long s = 0;
+    for (int v : d_) s += v;
+    return s;
+  }
+
+ private:
+  int n_ = 0, m_ = 0;
+  std::vector<int> d_;
+};
+
+class Lattice {
+ public:
+  explicit Lattice(int N, double K = -0.44068679350977147, uint64_t seed = 1, uint32_t replica = 0,
+                   int n_couplings = 2, int device = 0);
+  Lattice(int a, const SpinMatrix& spins, double K = -0.44068679350977147, uint64_t seed = 1);
+  ~Lattice();
+  Lattice(const Lattice&) = delete;
+  Lattice& operator=(const Lattice&) = delete;
+
+  int N_;
+  int n_spins_;
+  int a_;
+  SpinMatrix spins_;
+  bool mirror_spins_ = true;
+
+  // src/lattice.cpp:102-120 -> (S_nn, S_nnn) of the current configuration
+  std::vector<double> calc_interactions();
+  double calc_nearest_neighbor_interaction();
+
+  // push host edits of spins_ to the device / pull the device state
+  void upload_spins();
+  void sync_spins();
+
+  mcrg_ctx* ctx() const { return ctx_; }
+  void refresh() {
+    if (mirror_spins_) sync_spins();
+  }
+
+ private:
+  mcrg_ctx* ctx_ = nullptr;
+};
+
+class IsingModel {
+ public:
+  explicit IsingModel(double K);
+  ~IsingModel() {}
+
+  void equilibrate(std::shared_ptr<Lattice> pLattice, int n_samples_eq, bool write);
+  void sample_new_configuration(std::shared_ptr<Lattice> pLattice);
+  double calc_magnetization(std::shared_ptr<Lattice> pLattice);
+  double calc_energy(std::shared_ptr<Lattice> pLattice);
+
+ private:
+  double K_, P_;
+};
+
+class MonteCarloRenormalizationGroup {
+ public:
+  explicit MonteCarloRenormalizationGroup(int b);
+  ~MonteCarloRenormalizationGroup() {}
+
+  int b_;
+
+  // src/mcrg.cpp:22-144: prints and writes critical_exponent_N_<N>_K_<K>.txt
+  void calc_critical_exponent(int n_samples_eq, int n_samples, int N, double K);
+
+  // results of the last calc_critical_exponent (one entry per level pair)
+  std::vector<double> lambdas_;
+  std::vector<double> nus_;
+  uint64_t seed_ = 1;
+  int n_couplings_ = 2;
+  int device_ = 0;
+};
