@@ -248,20 +248,25 @@ def run_large(args, D: Dist) -> dict:
     }
 
 
-def run_batched(args, D: Dist) -> dict:
-    """4096 replicas, L ~ {16:.3, 32:.3, 64:.2, 128:.15, 256:.05}, K on a 33-point grid."""
+def batched_requests(M, n, sweeps, rank=0, seed0=1):
+    """The batched config: L ~ {16:.3, 32:.3, 64:.2, 128:.15, 256:.05}, K on a
+    33-point grid over [-0.49, -0.43], log2(L)-1 levels, measured every sweep."""
     import numpy as np
+    rng = np.random.default_rng(7 + rank)
+    Ls = rng.choice([16, 32, 64, 128, 256], size=n, p=[0.3, 0.3, 0.2, 0.15, 0.05])
+    Ks = np.linspace(-0.49, -0.43, 33)
+    return [M.make_request(int(L), float(Ks[i % 33]), seed=seed0 + i, replica=rank * n + i, n_eq=0,
+                           n_samples=sweeps, sweeps_between=1, n_couplings=2) for i, L in enumerate(Ls)]
+
+
+def run_batched(args, D: Dist) -> dict:
+    """4096 replicas in one batched call vs the same requests one lattice per launch."""
     import torch
     import mcrg_gb300 as M
 
     torch.cuda.set_device(D.local)
-    rng = np.random.default_rng(7 + D.rank)
-    Ls = rng.choice([16, 32, 64, 128, 256], size=args.replicas, p=[0.3, 0.3, 0.2, 0.15, 0.05])
-    Ks = np.linspace(-0.49, -0.43, 33)
-    reqs = [M.make_request(int(L), float(Ks[i % 33]), seed=1 + i, replica=D.rank * args.replicas + i,
-                           n_eq=0, n_samples=args.batch_sweeps, sweeps_between=1, n_couplings=2)
-            for i, L in enumerate(Ls)]
-    flips = float(sum(int(L) * int(L) for L in Ls)) * args.batch_sweeps
+    reqs = batched_requests(M, args.replicas, args.batch_sweeps, D.rank)
+    flips = float(sum(r.L * r.L for r in reqs)) * args.batch_sweeps
     for _ in range(args.warmup):
         M.batch_run(reqs, device=D.local)
     D.barrier()
@@ -272,13 +277,111 @@ def run_batched(args, D: Dist) -> dict:
     torch.cuda.synchronize()
     dt = D.max(time.perf_counter() - t0)
     value = D.world * flips * args.steps / dt / 1e9
+    solves = D.world * len(reqs) * args.steps / dt
+    plain = run_plain_subset(M, reqs[: args.plain_subset], D.local)
     return {"metric": "Gflips/s", "value": round(value, 2), "unit": "Gflips/s", "n_gpus": D.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-            "data": "synthetic", "solves_per_s": round(D.world * len(reqs) * args.steps / dt, 1),
-            "config": {"workload": "batched: %d replicas, L in {16..256}, K grid [-0.49,-0.43], %d sweeps each "
-                                   "(measured every sweep)" % (args.replicas, args.batch_sweeps),
-                       "parallelism": "replicas x%d" % D.world}}
+            "data": "synthetic", "solves_per_s": round(solves, 1),
+            "plain": plain, "batched_over_plain_solves": round(solves / D.world / plain["solves_per_s"], 1),
+            "config": {"workload": "batched: %d replicas, L in {16..256} (p = .3/.3/.2/.15/.05), K on 33 points in "
+                                   "[-0.49,-0.43], %d sweeps each, measured every sweep, 2 couplings"
+                                   % (args.replicas, args.batch_sweeps),
+                       "parallelism": "replicas x%d" % D.world,
+                       "equal_error": "batched and one-per-launch runs give bit-identical moment sums per seed"}}
+
+
+def run_plain_subset(M, reqs, device) -> dict:
+    """The plain GPU path: each request alone, one lattice per launch
+    (mcrg_alloc, mcrg_sweep, mcrg_measure, mcrg_free), back to back."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        lat = M.Lattice(r.L, r.K, seed=r.seed, replica=r.replica, n_couplings=r.n_couplings, device=device)
+        lat.sweep(r.n_eq)
+        lat.measure(r.n_samples, r.sweeps_between)
+        lat.close()
+    dt = time.perf_counter() - t0
+    flips = float(sum(r.L * r.L for r in reqs)) * reqs[0].n_samples
+    return {"solves_per_s": round(len(reqs) / dt, 2), "Gflips_per_s": round(flips / dt / 1e9, 3),
+            "requests": len(reqs), "seconds": round(dt, 3)}
+
+
+def run_plain(args, D: Dist) -> dict:
+    """One L = 64 lattice, one CTA per launch, 5 couplings (plain GPU config)."""
+    import torch
+    import mcrg_gb300 as M
+    torch.cuda.set_device(D.local)
+    lat = M.Lattice(64, KC, seed=1, replica=D.rank, n_couplings=5, device=D.local)
+    lat.sweep(args.warmup * args.plain_sweeps)
+    stream = torch.cuda.ExternalStream(lat.stream(), device=D.local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    D.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tot, bins = lat.measure(args.steps * args.plain_sweeps, 1, bin_size=args.plain_sweeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = D.max(e0.elapsed_time(e1))
+    from mcrg_gb300.tmatrix import jackknife
+    lam, err = jackknife(bins)
+    lat.close()
+    flips = 64.0 * 64 * args.plain_sweeps * args.steps
+    return {"metric": "Gflips/s", "value": round(D.world * flips / (ms * 1e-3) / 1e9, 3), "unit": "Gflips/s",
+            "n_gpus": D.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "lambda": [round(x, 5) for x in lam], "lambda_err": [round(x, 5) for x in err],
+            "config": {"workload": "plain: one L=64 lattice, one CTA, K=Kc, 5 couplings, 5 levels, measured every "
+                                   "sweep; step = %d sweeps (one error bin)" % args.plain_sweeps}}
+
+
+def run_served(args, D: Dist) -> dict:
+    """Poisson arrivals of MCRG requests (L log-uniform in {8..1024}, K ~ U[-0.50,-0.42],
+    sweeps log-uniform in [1e3, 1e5] scaled by --served-scale) into mcrg_server."""
+    import numpy as np
+    import torch
+    import mcrg_gb300 as M
+    torch.cuda.set_device(D.local)
+    rng = np.random.default_rng(11 + D.rank)
+    n = args.served_requests
+    Ls = 2 ** rng.integers(3, 11, size=n)
+    Ks = rng.uniform(-0.50, -0.42, size=n)
+    sw = np.exp(rng.uniform(np.log(1e3), np.log(1e5), size=n)) * args.served_scale
+    sw = np.maximum(1, sw.astype(np.int64))
+    gaps = rng.exponential(1.0 / args.served_rate, size=n)
+    reqs = [M.make_request(int(L), float(K), seed=100 + i, replica=i, n_eq=0, n_samples=int(s), sweeps_between=1,
+                           n_couplings=2) for i, (L, K, s) in enumerate(zip(Ls, Ks, sw))]
+    srv = M.Server(device=D.local, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)))
+    try:
+        t0 = time.perf_counter()
+        tickets = []
+        for r, g in zip(reqs, gaps):
+            target = (tickets[-1][1] if tickets else t0) + g
+            while time.perf_counter() < target:
+                pass
+            tickets.append((srv.submit(r), time.perf_counter()))
+        lat = []
+        for tk, ts in tickets:
+            res = srv.wait(tk, 600)
+            lat.append(res.done_s - res.submit_s)
+        wall = time.perf_counter() - t0
+    finally:
+        srv.close()
+    lat = np.array(lat)
+    flips = float(sum(int(L) * int(L) * int(s) for L, s in zip(Ls, sw)))
+    return {"metric": "MCRG solves/s", "value": round(n / wall, 2), "unit": "solves/s", "n_gpus": D.world,
+            "steps": 1, "warmup": 0, "ms_per_step": round(wall * 1e3, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "p50_latency_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_latency_s": round(float(np.percentile(lat, 99)), 4),
+            "Gflips_per_s": round(flips / wall / 1e9, 2),
+            "config": {"workload": "served: %d Poisson arrivals at %.0f/s, L log-uniform {8..1024}, K~U[-0.50,-0.42], "
+                                   "sweeps log-uniform [1e3,1e5] x %.3g, slots %d, budget %.0f GB"
+                                   % (n, args.served_rate, args.served_scale, args.served_slots,
+                                      args.served_budget_gb)}}
 
 
 # ---------------------------------------------------------------------------
@@ -333,12 +436,19 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=["large", "batched"])
+    ap.add_argument("--workload", default="large", choices=["large", "batched", "plain", "served"])
     ap.add_argument("--L", type=int, default=16384)
     ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--couplings", type=int, default=5)
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--batch-sweeps", type=int, default=1000)
+    ap.add_argument("--plain-subset", type=int, default=64)
+    ap.add_argument("--plain-sweeps", type=int, default=10000)
+    ap.add_argument("--served-requests", type=int, default=2000)
+    ap.add_argument("--served-rate", type=float, default=1000.0)
+    ap.add_argument("--served-scale", type=float, default=0.01)
+    ap.add_argument("--served-slots", type=int, default=512)
+    ap.add_argument("--served-budget-gb", type=float, default=150.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -369,10 +479,7 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    if args.workload == "large":
-        out = run_large(args, D)
-    else:
-        out = run_batched(args, D)
+    out = {"large": run_large, "batched": run_batched, "plain": run_plain, "served": run_served}[args.workload](args, D)
     if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads(args.L)
         cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads)

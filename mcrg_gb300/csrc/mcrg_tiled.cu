@@ -26,6 +26,7 @@
 #include <utility>
 
 #include "mcrg_ops.cuh"
+#include "mcrg_sweep_stream.cuh"
 #include "mcrg_sweep_tiled.cuh"
 #include "mcrg_tiled.cuh"
 
@@ -136,25 +137,58 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
 
 int g_num_sms = 0;
 
-// Tile-shape variants of the fused sweep; the autotuner picks one per
-// (L, device) by timing each eligible variant on the live lattice.
+// Variants of the fused sweep; the autotuner picks one per (L, device) by
+// timing each eligible variant on the live lattice.  "tiles" variants stage
+// TR x TC tiles with halos (any L); "stream" variants walk bands of
+// full-width rows (L = 16384 / R for R rows per step).
 struct Variant {
-  int TR, TC;
-  void (*kern)(const uint8_t*, uint8_t*, tiled::Params, uint32_t, int*);
+  const char* name;
+  int TR, TC;  // tile shape (TC = 0 marks a stream variant, TR = its R)
+  const void* kern;
   size_t smem;
 };
 
-#define MCRG_VARIANT(TR_, TC_) \
-  Variant { TR_, TC_, tiled::sweep_kernel<TR_, TC_, 256>, tiled::sweep_smem_bytes<TR_, TC_>() }
+#define TILE_VARIANT(TR_, TC_) \
+  Variant { "tiles", TR_, TC_, (const void*)tiled::sweep_kernel<TR_, TC_, 256>, tiled::sweep_smem_bytes<TR_, TC_>() }
+#define STREAM_VARIANT(R_) \
+  Variant { "stream", R_, 0, (const void*)stream::sweep_kernel<R_>, stream::smem_bytes<R_>() }
 
-const Variant kVariants[] = {MCRG_VARIANT(32, 1024), MCRG_VARIANT(16, 1024), MCRG_VARIANT(32, 512),
-                             MCRG_VARIANT(64, 512),  MCRG_VARIANT(16, 512),  MCRG_VARIANT(32, 256),
-                             MCRG_VARIANT(16, 2048)};
+const Variant kVariants[] = {TILE_VARIANT(32, 1024), TILE_VARIANT(16, 1024), TILE_VARIANT(32, 512),
+                             TILE_VARIANT(64, 512),  TILE_VARIANT(16, 512),  TILE_VARIANT(32, 256),
+                             TILE_VARIANT(16, 2048), STREAM_VARIANT(1),      STREAM_VARIANT(2),
+                             STREAM_VARIANT(4),      STREAM_VARIANT(8),      STREAM_VARIANT(16),
+                             STREAM_VARIANT(32)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-bool variant_fits(const Variant& v, int L) { return (L / 2) % v.TC == 0 && L % v.TR == 0; }
+bool variant_fits(const Variant& v, int L) {
+  if (v.TC == 0) return L * v.TR == 16384;
+  return (L / 2) % v.TC == 0 && L % v.TR == 0;
+}
 
-tiled::Params params_for(const TiledLattice* t, const Variant& v) {
+int ctas_for(const Variant& v, int work_items, int threads) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, threads, v.smem);
+  if (per_sm < 1) per_sm = 1;
+  int c = g_num_sms * per_sm;
+  return c < work_items ? c : work_items;
+}
+
+void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
+  const Variant& v = kVariants[vi];
+  if (v.TC == 0) {
+    stream::Params P;
+    memset(&P, 0, sizeof P);
+    P.key = t->key;
+    P.rep = t->replica;
+    P.acc = t->acc;
+    // bands of at least 8R rows, at most one CTA per SM
+    int bands = t->L / (8 * v.TR);
+    if (bands > g_num_sms) bands = g_num_sms;
+    if (bands < 1) bands = 1;
+    void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
+    cudaLaunchKernel(v.kern, dim3(bands), dim3(stream::kThreads), args, v.smem, s);
+    return;
+  }
   tiled::Params P;
   memset(&P, 0, sizeof P);
   P.L = t->L;
@@ -164,21 +198,8 @@ tiled::Params params_for(const TiledLattice* t, const Variant& v) {
   P.key = t->key;
   P.rep = t->replica;
   P.acc = t->acc;
-  return P;
-}
-
-int ctas_for(const Variant& v, int n_tiles) {
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, 256, v.smem);
-  if (per_sm < 1) per_sm = 1;
-  int c = g_num_sms * per_sm;
-  return c < n_tiles ? c : n_tiles;
-}
-
-void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
-  const Variant& v = kVariants[vi];
-  const tiled::Params P = params_for(t, v);
-  v.kern<<<ctas_for(v, P.n_tiles), 256, v.smem, s>>>(in, out, P, tt, t->d_status);
+  void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
+  cudaLaunchKernel(v.kern, dim3(ctas_for(v, P.n_tiles, 256)), dim3(256), args, v.smem, s);
 }
 
 int first_tail_level(int L) {
@@ -254,7 +275,8 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   cudaGetDevice(&dev);
   if (const char* force = getenv("MCRG_TILE")) {
     int tr = 0, tc = 0;
-    if (sscanf(force, "%dx%d", &tr, &tc) == 2)
+    if (force[0] == 's' && sscanf(force + 1, "%d", &tr) == 1) tc = 0;
+    if (force[0] == 's' || sscanf(force, "%dx%d", &tr, &tc) == 2)
       for (int v = 0; v < kNumVariants; ++v)
         if (kVariants[v].TR == tr && kVariants[v].TC == tc && variant_fits(kVariants[v], t->L)) return v;
   }

@@ -302,3 +302,47 @@ def test_device_chain_matches_reference_L8(M, golden):
     for l in range(2):
         assert abs(est[l] - mu[l]) < 5 * math.sqrt(sd[l] ** 2 + err[l] ** 2), (l, est, err, mu, sd)
     lat.close()
+
+
+# --------------------------------------------------------------------------
+# every sweep variant of the HBM path (tile shapes and band streaming)
+# --------------------------------------------------------------------------
+def _variants_for(N):
+    tiles = [(32, 1024), (16, 1024), (32, 512), (64, 512), (16, 512), (32, 256), (16, 2048)]
+    out = ["%dx%d" % (tr, tc) for tr, tc in tiles if (N // 2) % tc == 0 and N % tr == 0]
+    if 16384 % N == 0:
+        out.append("s%d" % (16384 // N))
+    return out
+
+
+@pytest.mark.parametrize("N", [512, 1024, 2048, 4096])
+def test_every_sweep_variant_bit_exact(M, N, monkeypatch):
+    init = O.init_spins(N, 77, 4)
+    ref = O.sweep(init, KC, 77, 4, 0, 2)
+    for v in _variants_for(N):
+        monkeypatch.setenv("MCRG_TILE", v)
+        lat = M.Lattice(N, KC, seed=77, replica=4)
+        lat.sweep(2)
+        got = lat.spins_
+        assert lat.tile_shape() is not None
+        lat.close()
+        np.testing.assert_array_equal(got, ref, err_msg="variant %s" % v)
+
+
+def test_full_size_lattice_one_sweep(M, monkeypatch):
+    """L = 16384 (the benchmark lattice): one sweep of each main variant and
+    the level-0 coupling sums, bit-exact against the oracle."""
+    N = 16384
+    init = O.init_spins(N, 5, 0)
+    ref = O.sweep(init, KC, 5, 0, 0, 1)
+    ref_S = O.couplings(ref, 5)
+    for v in ("s1", "32x1024"):
+        monkeypatch.setenv("MCRG_TILE", v)
+        lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
+        lat.sweep(1)
+        got = lat.spins_
+        S = lat.interactions()
+        lat.close()
+        assert np.array_equal(got, ref), "variant %s differs at %d sites" % (v, int((got != ref).sum()))
+        np.testing.assert_array_equal(S[0], ref_S)
+        del got
