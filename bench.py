@@ -267,13 +267,14 @@ def run_batched(args, D: Dist) -> dict:
     torch.cuda.set_device(D.local)
     reqs = batched_requests(M, args.replicas, args.batch_sweeps, D.rank)
     flips = float(sum(r.L * r.L for r in reqs)) * args.batch_sweeps
+    creqs = (M._abi.Request * len(reqs))(*reqs)
     for _ in range(args.warmup):
-        M.batch_run(reqs, device=D.local)
+        M.batch_run(creqs, device=D.local, raw=True)
     D.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        M.batch_run(reqs, device=D.local)
+        M.batch_run(creqs, device=D.local, raw=True)
     torch.cuda.synchronize()
     dt = D.max(time.perf_counter() - t0)
     value = D.world * flips * args.steps / dt / 1e9

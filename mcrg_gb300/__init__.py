@@ -231,12 +231,19 @@ def make_request(L: int, K: float, seed: int, replica: int = 0, n_eq: int = 0, n
     return _abi.Request(L, n_levels, n_couplings, 0, float(K), seed, replica, 0, n_eq, n_samples, sweeps_between)
 
 
-def batch_run(requests: list[_abi.Request], device: int = 0, use_graph: bool = True):
-    n = len(requests)
-    reqs = (_abi.Request * n)(*requests)
+def batch_run(requests, device: int = 0, use_graph: bool = True, raw: bool = False):
+    """mcrg_batch_run.  requests: a list of Request or a ctypes Request array.
+    raw=True returns the ctypes Result array without converting the moments."""
+    if isinstance(requests, C.Array):
+        reqs, n = requests, len(requests)
+    else:
+        n = len(requests)
+        reqs = (_abi.Request * n)(*requests)
     res = (_abi.Result * n)()
     rc = lib().mcrg_batch_run(reqs, n, res, device, 1 if use_graph else 0)
     check(rc, "mcrg_batch_run")
+    if raw:
+        return res
     return [(int(r.status), moments_from_c(r.moments) if r.status == 0 else None) for r in res]
 
 

@@ -17,6 +17,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <ctime>
+#include <algorithm>
 #include <deque>
 #include <map>
 #include <mutex>
@@ -121,6 +122,72 @@ int run_tiled_request(const mcrg_request* r, int device, mcrg_moments* out) {
   return rc;
 }
 
+// Device buffers, pinned staging and streams of mcrg_batch_run, kept per
+// device between calls so a batch does not pay allocation or stream set-up.
+constexpr int kMaxGroups = 8;
+
+struct BatchWorkspace {
+  std::mutex mu;
+  bool ready = false;
+  uint8_t* d_state = nullptr;
+  size_t state_cap = 0;
+  mcrg_moments* d_bins = nullptr;
+  mcrg_moments* h_bins = nullptr;  // pinned
+  size_t bins_cap = 0;
+  ChainJob* d_jobs = nullptr;
+  ChainJob* h_jobs = nullptr;      // pinned
+  size_t jobs_cap = 0;
+  cudaStream_t s0 = nullptr;
+  cudaStream_t ss[kMaxGroups] = {};
+  cudaEvent_t ev[kMaxGroups + 1] = {};
+
+  int reserve(size_t state_bytes, size_t n_bins, size_t n_jobs) {
+    if (!ready) {
+      if (cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
+      for (auto& x : ss)
+        if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
+      for (auto& e : ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return MCRG_EIO;
+      ready = true;
+    }
+    if (state_bytes > state_cap) {
+      cudaFree(d_state);
+      d_state = nullptr;
+      state_cap = 0;
+      if (cudaMalloc(&d_state, state_bytes) != cudaSuccess) return MCRG_ENOMEM;
+      state_cap = state_bytes;
+    }
+    if (n_bins > bins_cap) {
+      cudaFree(d_bins);
+      cudaFreeHost(h_bins);
+      d_bins = nullptr;
+      h_bins = nullptr;
+      bins_cap = 0;
+      if (cudaMalloc(&d_bins, sizeof(mcrg_moments) * n_bins) != cudaSuccess ||
+          cudaMallocHost(&h_bins, sizeof(mcrg_moments) * n_bins) != cudaSuccess)
+        return MCRG_ENOMEM;
+      bins_cap = n_bins;
+    }
+    if (n_jobs > jobs_cap) {
+      cudaFree(d_jobs);
+      cudaFreeHost(h_jobs);
+      d_jobs = nullptr;
+      h_jobs = nullptr;
+      jobs_cap = 0;
+      if (cudaMalloc(&d_jobs, sizeof(ChainJob) * n_jobs) != cudaSuccess ||
+          cudaMallocHost(&h_jobs, sizeof(ChainJob) * n_jobs) != cudaSuccess)
+        return MCRG_ENOMEM;
+      jobs_cap = n_jobs;
+    }
+    return MCRG_OK;
+  }
+};
+
+BatchWorkspace& workspace(int device) {
+  static BatchWorkspace ws[64];
+  return ws[device & 63];
+}
+
 }  // namespace
 
 extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* results, int32_t device,
@@ -156,78 +223,70 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
   }
   int rc = MCRG_OK;
   if (!groups.empty()) {
-    uint8_t* d_state = nullptr;
-    mcrg_moments* d_bins = nullptr;
-    ChainJob* d_jobs = nullptr;
-    std::vector<ChainJob> jobs;
+    BatchWorkspace& w = workspace(device);
+    std::lock_guard<std::mutex> lk(w.mu);
     std::vector<std::pair<int, int>> ranges;  // (first job, count) per group
     std::vector<int> order;                   // job index -> request index
-    if (cudaMalloc(&d_state, state_bytes + 16) != cudaSuccess ||
-        cudaMalloc(&d_bins, sizeof(mcrg_moments) * (size_t)(total_bins > 0 ? total_bins : 1)) != cudaSuccess) {
-      rc = MCRG_ENOMEM;
-    }
+    const size_t n_jobs = (size_t)n - tiled.size() - (size_t)std::count_if(results, results + n, [](const mcrg_result& r) {
+                            return r.status != MCRG_OK;
+                          });
+    const size_t nb = (size_t)(total_bins > 0 ? total_bins : 1);
+    rc = w.reserve(state_bytes + 16, nb, n_jobs);
     if (!rc) {
       // largest sides first so the longest chains start earliest
+      size_t k = 0;
       for (auto it = groups.rbegin(); it != groups.rend(); ++it) {
-        ranges.push_back({(int)jobs.size(), (int)it->second.size()});
+        ranges.push_back({(int)k, (int)it->second.size()});
         for (int i : it->second) {
-          ChainJob j;
-          fill_job(&j, &reqs[i], nl[i], d_state + state_off[i], d_bins + bin_off[i]);
-          jobs.push_back(j);
+          fill_job(&w.h_jobs[k++], &reqs[i], nl[i], w.d_state + state_off[i], w.d_bins + bin_off[i]);
           order.push_back(i);
         }
       }
-      if (cudaMalloc(&d_jobs, sizeof(ChainJob) * jobs.size()) != cudaSuccess) rc = MCRG_ENOMEM;
-    }
-    cudaStream_t s0 = nullptr;
-    std::vector<cudaStream_t> ss(ranges.size(), nullptr);
-    std::vector<cudaEvent_t> ev(ranges.size() + 1, nullptr);
-    if (!rc) {
-      cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
-      for (auto& s : ss) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-      for (auto& e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-      cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(ChainJob) * jobs.size(), cudaMemcpyHostToDevice, s0);
-      cudaMemsetAsync(d_bins, 0, sizeof(mcrg_moments) * (size_t)(total_bins > 0 ? total_bins : 1), s0);
+      cudaStream_t s0 = w.s0;
+      cudaMemcpyAsync(w.d_jobs, w.h_jobs, sizeof(ChainJob) * n_jobs, cudaMemcpyHostToDevice, s0);
+      cudaMemsetAsync(w.d_bins, 0, sizeof(mcrg_moments) * nb, s0);
       cudaGraph_t graph = nullptr;
       cudaGraphExec_t exec = nullptr;
       if (use_graph) cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
-      cudaEventRecord(ev.back(), s0);
+      cudaEventRecord(w.ev[kMaxGroups], s0);
       for (size_t g = 0; g < ranges.size(); ++g) {
-        cudaStreamWaitEvent(ss[g], ev.back(), 0);
-        const ChainJob& j0 = jobs[(size_t)ranges[g].first];
+        cudaStream_t sg = w.ss[g % kMaxGroups];
+        cudaStreamWaitEvent(sg, w.ev[kMaxGroups], 0);
+        const ChainJob& j0 = w.h_jobs[(size_t)ranges[g].first];
         int maxlev = 0;
-        for (int k = 0; k < ranges[g].second; ++k) maxlev = std::max(maxlev, jobs[(size_t)ranges[g].first + k].n_levels);
-        if (launch_chain(d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads, ss[g]) != cudaSuccess)
+        for (int q = 0; q < ranges[g].second; ++q) maxlev = std::max(maxlev, w.h_jobs[(size_t)ranges[g].first + q].n_levels);
+        if (launch_chain(w.d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads,
+                         sg) != cudaSuccess)
           rc = MCRG_EIO;
-        cudaEventRecord(ev[g], ss[g]);
-        cudaStreamWaitEvent(s0, ev[g], 0);
+        cudaEventRecord(w.ev[g % kMaxGroups], sg);
+        cudaStreamWaitEvent(s0, w.ev[g % kMaxGroups], 0);
       }
       if (use_graph) {
         if (cudaStreamEndCapture(s0, &graph) != cudaSuccess ||
             cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess || cudaGraphLaunch(exec, s0) != cudaSuccess)
           rc = MCRG_EIO;
       }
-      std::vector<mcrg_moments> h((size_t)(total_bins > 0 ? total_bins : 0));
       if (total_bins > 0)
-        cudaMemcpyAsync(h.data(), d_bins, sizeof(mcrg_moments) * (size_t)total_bins, cudaMemcpyDeviceToHost, s0);
+        cudaMemcpyAsync(w.h_bins, w.d_bins, sizeof(mcrg_moments) * (size_t)total_bins, cudaMemcpyDeviceToHost, s0);
       if (cudaStreamSynchronize(s0) != cudaSuccess) rc = MCRG_EIO;
       const double t_done = mono_s();
       for (int i : order) {
+        const int64_t nbi = n_dev_bins(&reqs[i]);
+        if (nbi == 1) {
+          results[i].moments = w.h_bins[(size_t)bin_off[i]];
+        } else {
+          results[i].moments.n_levels = nl[i];
+          results[i].moments.n_couplings = reqs[i].n_couplings;
+          for (int64_t q = 0; q < nbi; ++q) add_into(&results[i].moments, &w.h_bins[(size_t)(bin_off[i] + q)]);
+        }
         results[i].moments.n_levels = nl[i];
         results[i].moments.n_couplings = reqs[i].n_couplings;
-        for (int64_t q = 0; q < n_dev_bins(&reqs[i]); ++q) add_into(&results[i].moments, &h[(size_t)(bin_off[i] + q)]);
         results[i].done_s = t_done;
         if (rc) results[i].status = rc;
       }
       if (exec) cudaGraphExecDestroy(exec);
       if (graph) cudaGraphDestroy(graph);
-      for (auto& e : ev) cudaEventDestroy(e);
-      for (auto& s : ss) cudaStreamDestroy(s);
-      cudaStreamDestroy(s0);
     }
-    cudaFree(d_jobs);
-    cudaFree(d_bins);
-    cudaFree(d_state);
   }
   for (int i : tiled) {
     results[i].status = run_tiled_request(&reqs[i], device, &results[i].moments);

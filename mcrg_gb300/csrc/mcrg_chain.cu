@@ -22,11 +22,11 @@ namespace mcrg {
 
 // One sweep of a resident lattice: colour 0, then colour 1.
 __device__ __noinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key key, uint32_t rep, const Accept& acc,
-                                         bool vec, int tid, int T) {
+                                         bool vec, int tid, int T, uint32_t* scratch) {
   for (int c = 0; c < 2; ++c) {
     if (vec) {
-      if (L >= 32) sweep_colour_vec<4>(lat, L, c, t, key, rep, acc, tid, T);
-      else sweep_colour_vec<2>(lat, L, c, t, key, rep, acc, tid, T);
+      if (L >= 32) sweep_colour_vec<4>(lat, L, c, t, key, rep, acc, tid, T, scratch);
+      else sweep_colour_vec<2>(lat, L, c, t, key, rep, acc, tid, T, scratch);
     } else {
       sweep_colour_scalar(lat, L, c, t, key, rep, acc, tid, T);
     }
@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
   long long* macc = reinterpret_cast<long long*>(smem + plan.acc_off);
   const int E = plan.E;
+  uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (threadIdx.x >> 5) * kOpenPerWarp;
   const bool vec = acc.fast && L >= 16;
 
   // ---- configuration into shared memory
@@ -83,9 +84,9 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   __syncthreads();
 
   uint32_t t = J.t0;
-  for (int64_t s = 0; s < J.n_eq; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T);
+  for (int64_t s = 0; s < J.n_eq; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
   for (int64_t n = 0; n < J.n_samples; ++n) {
-    for (int64_t s = 0; s < J.sweeps_between; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T);
+    for (int64_t s = 0; s < J.sweeps_between; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
     // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;

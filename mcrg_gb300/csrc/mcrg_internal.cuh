@@ -31,6 +31,7 @@ struct SmemPlan {
   int s_off;    // int32 S[(MCRG_MAX_LEVELS+1) * MCRG_MAX_COUPLINGS]
   int tab_off;  // int2 per moment entry: (x | y << 16, output index)
   int acc_off;  // int64 per moment entry
+  int scr_off;  // uint32 open-site scratch: 64 per warp, up to 8 warps
   int E;        // moment entries
   int bytes;
 };
@@ -49,6 +50,8 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
   off += ((p.E * 8 + 15) / 16) * 16;
   p.acc_off = off;
   off += p.E * 8;
+  p.scr_off = off;
+  off += 8 * 64 * 4;
   p.bytes = (off + 15) / 16 * 16;
   return p;
 }

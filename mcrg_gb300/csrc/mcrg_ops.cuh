@@ -83,6 +83,23 @@ __device__ __forceinline__ uint32_t update_chunk(uint32_t (&tw)[NW], const uint3
   return open;
 }
 
+// Same update with the side-neighbour direction fixed at compile time (Q = q).
+template <int NW, int Q>
+__device__ __forceinline__ uint32_t update_chunk_q(uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
+                                                   const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t prv,
+                                                   uint32_t nxt, const uint4& R, const Accept& a) {
+  uint32_t open = 0;
+#pragma unroll
+  for (int j = 0; j < NW; ++j) {
+    uint32_t tie, side;
+    if (Q) side = __funnelshift_r(mw[j], j + 1 < NW ? mw[j + 1] : nxt, 8);
+    else side = __funnelshift_r(j > 0 ? mw[j - 1] : prv, mw[j], 24);
+    tw[j] = swar_update(tw[j], uw[j], dw[j], mw[j], side, u4get(R, j), a, &tie);
+    open |= tie >> j;
+  }
+  return open;
+}
+
 // Chunk byte of bit p of an open-site mask.
 __device__ __forceinline__ int open_byte(int p) { return 4 * (7 - (p & 7)) + (p >> 3); }
 
@@ -98,12 +115,70 @@ __device__ __forceinline__ bool resolve_open(uint32_t t, uint32_t n0, uint32_t n
   return (u4get(lo, k & 3) & 0xFFFFFFu) < (a.thr[m] & 0xFFFFFFu);
 }
 
+// Descriptors one warp resolves cooperatively per pass (scratch entries).
+constexpr int kOpenPerWarp = 64;
+
+// Resolves the open sites of the warp's chunks of one round.  om[r] is the
+// open mask of this lane's chunk r (row i_r, first byte k_r).  The sites are
+// spread over the warp's lanes (one Philox block each) instead of each owner
+// resolving its own, which would serialise the warp.  All lanes must call it.
+template <int NW>
+__device__ __forceinline__ void warp_resolve_resident(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
+                                                      const Accept& a, const uint32_t (&om)[8], int base, int tid,
+                                                      int T, int cpr, uint32_t* scratch) {
+  constexpr int CB = 4 * NW;
+  const int half = n / 2, lane = threadIdx.x & 31;
+  uint8_t* Cc = lat + (size_t)c * n * half;
+  const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
+  int cnt = 0;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) cnt += __popc(om[r]);
+  if (__ballot_sync(0xFFFFFFFFu, cnt != 0) == 0) return;
+  int off = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xFFFFFFFFu, off, d);
+    if (lane >= d) off += y;
+  }
+  const int total = __shfl_sync(0xFFFFFFFFu, off, 31);
+  int slot = off - cnt;
+  auto resolve = [&](int i, int k) {
+    const int q = (i + c) & 1;
+    uint8_t* sp = Cc + (size_t)i * half + k;
+    const uint8_t* orow = Oc + (size_t)i * half;
+    if (resolve_open(*sp, Oc[(size_t)((i - 1) & (n - 1)) * half + k], Oc[(size_t)((i + 1) & (n - 1)) * half + k],
+                     orow[(k - 1 + q) & (half - 1)], orow[(k + q) & (half - 1)], key, rep, (uint32_t)c, i, k, t, a))
+      *sp ^= 1u;
+  };
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    uint32_t bits = om[r];
+    if (!bits) continue;
+    const int task = base + tid + r * T;
+    const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB;
+    while (bits) {
+      const int p = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int k = k0 + open_byte(p);
+      if (slot < kOpenPerWarp) scratch[slot] = ((uint32_t)i << 13) | (uint32_t)k;
+      else resolve(i, k);
+      ++slot;
+    }
+  }
+  __syncwarp();
+  for (int j = lane; j < min(total, kOpenPerWarp); j += 32) {
+    const uint32_t d = scratch[j];
+    resolve((int)(d >> 13), (int)(d & 0x1FFFu));
+  }
+  __syncwarp();
+}
+
 // Vector sweep of colour c of a resident n x n lattice (n >= 16).  Threads
-// take chunks in rounds of up to 8, keep the open-site masks in registers and
-// resolve their own open sites at the end of each round.
+// take chunks in rounds of up to 8 per thread; the open sites of a round are
+// resolved by the warp together at the end of the round.
 template <int NW>
 __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
-                                 const Accept& a, int tid, int T) {
+                                 const Accept& a, int tid, int T, uint32_t* scratch) {
   constexpr int CB = 4 * NW;  // chunk bytes
   const int half = n / 2, cpr = half / CB, ntask = n * cpr;
   uint8_t* Cc = lat + (size_t)c * n * half;
@@ -131,23 +206,7 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
         store_words<NW>(tp, tw);
       }
     }
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      uint32_t bits = om[r];
-      if (!bits) continue;
-      const int task = base + tid + r * T;
-      const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB, q = (i + c) & 1;
-      while (bits) {
-        const int p = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const int k = k0 + open_byte(p);
-        uint8_t* sp = Cc + (size_t)i * half + k;
-        const uint8_t* orow = Oc + (size_t)i * half;
-        if (resolve_open(*sp, Oc[(size_t)((i - 1) & (n - 1)) * half + k], Oc[(size_t)((i + 1) & (n - 1)) * half + k],
-                         orow[(k - 1 + q) & (half - 1)], orow[(k + q) & (half - 1)], key, rep, (uint32_t)c, i, k, t, a))
-          *sp ^= 1u;
-      }
-    }
+    warp_resolve_resident<NW>(lat, n, c, t, key, rep, a, om, base, tid, T, cpr, scratch);
   }
 }
 
