@@ -83,23 +83,6 @@ __device__ __forceinline__ uint32_t update_chunk(uint32_t (&tw)[NW], const uint3
   return open;
 }
 
-// Same update with the side-neighbour direction fixed at compile time (Q = q).
-template <int NW, int Q>
-__device__ __forceinline__ uint32_t update_chunk_q(uint32_t (&tw)[NW], const uint32_t (&uw)[NW],
-                                                   const uint32_t (&dw)[NW], const uint32_t (&mw)[NW], uint32_t prv,
-                                                   uint32_t nxt, const uint4& R, const Accept& a) {
-  uint32_t open = 0;
-#pragma unroll
-  for (int j = 0; j < NW; ++j) {
-    uint32_t tie, side;
-    if (Q) side = __funnelshift_r(mw[j], j + 1 < NW ? mw[j + 1] : nxt, 8);
-    else side = __funnelshift_r(j > 0 ? mw[j - 1] : prv, mw[j], 24);
-    tw[j] = swar_update(tw[j], uw[j], dw[j], mw[j], side, u4get(R, j), a, &tie);
-    open |= tie >> j;
-  }
-  return open;
-}
-
 // Chunk byte of bit p of an open-site mask.
 __device__ __forceinline__ int open_byte(int p) { return 4 * (7 - (p & 7)) + (p >> 3); }
 

@@ -62,7 +62,7 @@ constexpr int kAhead = 5;      // stages in flight ahead of the compute
 
 template <int R>
 constexpr size_t smem_bytes() {
-  return 128 + 2 * (size_t)(8 * R) * (size_t)(kThreads / R) * 16 + (kThreads / 32) * 64 * 4;
+  return 128 + 2 * (size_t)(8 * R) * (size_t)(kThreads / R) * 16;
 }
 
 // Ring of row slots of one CTA (rows b0-2 .. b1+1 map to slot (r-b0+2) mod SLOTS).
@@ -120,110 +120,36 @@ __device__ __forceinline__ bool wait_stage(uint64_t* bar, int k) {
   return ok;
 }
 
-// One open site resolved exactly: returns true when it flips.
+// Colour-0 chunk c of row r (update in place, then resolve its open sites).
 template <int R>
-__device__ __forceinline__ void resolve_site(const Ring<R>& g, uint32_t colour, int r, int k, const Params& P,
-                                             uint32_t tt) {
+__device__ __forceinline__ void black_chunk(const Ring<R>& g, int r, int c, const Params& P, uint32_t tt) {
   constexpr int H = Ring<R>::H, L = Ring<R>::L;
-  uint8_t* row = colour ? g.w(r) : g.b(r);
-  const uint8_t* up = colour ? g.b(r - 1) : g.w(r - 1);
-  const uint8_t* dn = colour ? g.b(r + 1) : g.w(r + 1);
-  const uint8_t* mid = colour ? g.b(r) : g.w(r);
-  const int gr = (r + L) & (L - 1), q = (gr + (int)colour) & 1;
-  if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], P.key, P.rep, colour, gr,
-                   k, tt, P.acc))
-    row[k] ^= 1u;
-}
-
-// Open-site descriptor: colour << 31 | (row - b0 + 2) << 13 | k.
-constexpr int kWarpOpen = 64;  // descriptors one warp resolves cooperatively per pass
-
-// Resolves the open sites of the warp: this lane's colour-0 chunk (row rb)
-// and its deferred colour-1 chunk (row rw), both at chunk byte offset k0.
-// Sites are spread over the warp's lanes (one Philox block each) instead of
-// each owner resolving its own, which would serialise the warp.
-template <int R>
-__device__ __forceinline__ void warp_resolve(const Ring<R>& g, uint32_t* scratch, uint32_t bits_b, int rb,
-                                             uint32_t bits_w, int rw, int k0, const Params& P, uint32_t tt) {
-  const int lane = threadIdx.x & 31;
-  const int cnt = __popc(bits_b) + __popc(bits_w);
-  if (__ballot_sync(0xFFFFFFFFu, cnt != 0) == 0) return;
-  int off = cnt;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int y = __shfl_up_sync(0xFFFFFFFFu, off, d);
-    if (lane >= d) off += y;
-  }
-  const int total = __shfl_sync(0xFFFFFFFFu, off, 31);
-  int slot = off - cnt;
-  while (bits_b) {
-    const int p = __ffs(bits_b) - 1;
-    bits_b &= bits_b - 1;
-    const int k = k0 + open_byte(p);
-    if (slot < kWarpOpen) scratch[slot] = ((uint32_t)(rb - g.b0 + 2) << 13) | (uint32_t)k;
-    else resolve_site<R>(g, 0u, rb, k, P, tt);
-    ++slot;
-  }
-  while (bits_w) {
-    const int p = __ffs(bits_w) - 1;
-    bits_w &= bits_w - 1;
-    const int k = k0 + open_byte(p);
-    if (slot < kWarpOpen) scratch[slot] = 0x80000000u | ((uint32_t)(rw - g.b0 + 2) << 13) | (uint32_t)k;
-    else resolve_site<R>(g, 1u, rw, k, P, tt);
-    ++slot;
-  }
-  __syncwarp();
-  for (int j = lane; j < min(total, kWarpOpen); j += 32) {
-    const uint32_t d = scratch[j];
-    resolve_site<R>(g, d >> 31, (int)((d >> 13) & 0x3FFFFu) + g.b0 - 2, (int)(d & 0x1FFFu), P, tt);
-  }
-  __syncwarp();
-}
-
-// SWAR update of one chunk at k0 of `row` from the other colour's rows.
-// The parity q of the row is uniform across a warp (a warp never straddles
-// rows), so the two directions are separate code paths.
-template <int R, int QT>
-__device__ __forceinline__ uint32_t chunk_step(uint32_t (&tw)[4], const uint8_t* row, const uint8_t* up,
-                                               const uint8_t* dn, const uint8_t* mid, int k0, int q, const uint4& Rn,
-                                               const Accept& a, uint32_t (&mw)[4]) {
-  constexpr int H = Ring<R>::H;
-  uint32_t uw[4], dw[4];
+  const int k0 = c * 16;
+  uint8_t* row = g.b(r);
+  const uint8_t* mid = g.w(r);
+  const uint8_t* up = g.w(r - 1);
+  const uint8_t* dn = g.w(r + 1);
+  uint32_t tw[4], uw[4], dw[4], mw[4];
   load_words4(row + k0, tw);
   load_words4(up + k0, uw);
   load_words4(dn + k0, dw);
   load_words4(mid + k0, mw);
-  if (QT) {  // two code paths, direction fixed at compile time (the branch is warp-uniform)
-    if (q) return update_chunk_q<4, 1>(tw, uw, dw, mw, 0u, load_word(mid + ((k0 + 16) & (H - 1))), Rn, a);
-    return update_chunk_q<4, 0>(tw, uw, dw, mw, load_word(mid + ((k0 - 4) & (H - 1))), 0u, Rn, a);
-  }
-  return update_chunk<4>(tw, uw, dw, mw, load_word(mid + ((k0 - 4) & (H - 1))), load_word(mid + ((k0 + 16) & (H - 1))),
-                         (uint32_t)q, Rn, a);
-}
-
-template <int R>
-__device__ __forceinline__ uint4 black_draw(int r, int c, const Params& P, uint32_t tt) {
-  constexpr int L = Ring<R>::L;
-  return stream_block(P.key, P.rep, P_SWEEP_HI, 0u, (uint32_t)((r + L) & (L - 1)), (uint32_t)c, tt);
-}
-
-// Per-thread resolution of the open sites of one chunk (the owner resolves).
-template <int R>
-__device__ __noinline__ void own_resolve(const Ring<R>& g, uint32_t colour, int r, int k0, uint32_t bits,
-                                         const Params& P, uint32_t tt) {
+  const uint32_t prv = load_word(mid + ((k0 - 4) & (H - 1))), nxt = load_word(mid + ((k0 + 16) & (H - 1)));
+  const int gr = (r + L) & (L - 1), q = gr & 1;
+  const uint4 Rn = stream_block(P.key, P.rep, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)c, tt);
+  uint32_t bits = update_chunk<4>(tw, uw, dw, mw, prv, nxt, (uint32_t)q, Rn, P.acc);
+  store_words<4>(row + k0, tw);
   while (bits) {
     const int p = __ffs(bits) - 1;
     bits &= bits - 1;
-    resolve_site<R>(g, colour, r, k0 + open_byte(p), P, tt);
+    const int k = k0 + open_byte(p);
+    if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], P.key, P.rep, 0u, gr,
+                     k, tt, P.acc))
+      row[k] ^= 1u;
   }
 }
 
-// PIPE: compute the next step's draws alongside this step's update.
-// COOP: resolve open sites warp-cooperatively once per step (colour-1 sites
-//       deferred by one step) instead of by their owners right away.
-// QT:   side-neighbour direction as two compile-time code paths instead of
-//       selects.
-template <int R, int PIPE, int COOP, int QT>
+template <int R>
 __global__ void __launch_bounds__(kThreads, 1)
     sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, Params P, uint32_t tt,
                  int* __restrict__ status) {
@@ -235,14 +161,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   Ring<R> g;
   g.Ws = smem + 128;
   g.Bs = g.Ws + SLOTS * H;
-  uint32_t* scratch = reinterpret_cast<uint32_t*>(g.Bs + SLOTS * H) + (tid >> 5) * kWarpOpen;
   g.b0 = (int)(((long long)blockIdx.x * L) / gridDim.x);
   const int b0 = g.b0;
   const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
   const int nsteps = (b1 - b0 + R - 1) / R;
-  // with one row per step every thread of the block works on the same row
-  const int rr = (R == 1) ? 0 : tid / CPR;
-  const int c = (R == 1) ? tid : tid % CPR, k0 = c * 16;
 
   if (tid < kStages) mbar_init(&bar[tid], 1);
   if (tid == 0) fence_mbar_init();
@@ -252,49 +174,15 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   // ---- prologue: colour 0 on rows b0-1 and b0
   bool ok = wait_stage(bar, -1);
-  for (int x = tid; x < 2 * CPR; x += kThreads) {
-    const int r = b0 - 1 + x / CPR, cc = x % CPR;
-    uint32_t tw[4], mw[4];
-    uint8_t* row = g.b(r);
-    const int q = ((r + L) & (L - 1)) & 1;
-    const uint32_t bits = chunk_step<R, QT>(tw, row, g.w(r - 1), g.w(r + 1), g.w(r), cc * 16, q,
-                                        black_draw<R>(r, cc, P, tt), P.acc, mw);
-    if (ok) store_words<4>(row + cc * 16, tw);
-    if (COOP) warp_resolve<R>(g, scratch, ok ? bits : 0u, r, 0u, r, cc * 16, P, tt);
-    else if (ok && bits) own_resolve<R>(g, 0u, r, cc * 16, bits, P, tt);
-  }
+  if (ok)
+    for (int x = tid; x < 2 * CPR; x += kThreads) black_chunk<R>(g, b0 - 1 + x / CPR, x % CPR, P, tt);
 
-  uint4 Rb = black_draw<R>(b0 + 1 + rr, c, P, tt);
-  uint4 Rw = stream_block(P.key, P.rep, P_SWEEP_HI, 1u, (uint32_t)(b0 + rr), (uint32_t)c, tt);
-  uint32_t pend = 0;  // open colour-1 sites of the previous step (row r - R), COOP only
   for (int s = 0; s < nsteps; ++s) {
     if (!wait_stage(bar, s)) ok = false;
-    const int rb = b0 + s * R + 1 + rr;  // colour-0 row of this step
-    const int r = rb - 1;                // colour-1 row of this step
-    uint4 Rb_next, Rw_next;
-    if (PIPE) {
-      Rb_next = black_draw<R>(rb + R, c, P, tt);
-      Rw_next = stream_block(P.key, P.rep, P_SWEEP_HI, 1u, (uint32_t)((r + R) & (L - 1)), (uint32_t)c, tt);
-    } else {
-      Rb = black_draw<R>(rb, c, P, tt);
-    }
-    // ---- colour 0 (rows past b1 in the last step run on stale slots and are not stored)
-    uint32_t bits_b;
+    // ---- colour 0, rows b0+sR+1 .. b0+(s+1)R (<= b1)
     {
-      uint8_t* row = g.b(rb);
-      const int q = ((rb + L) & (L - 1)) & 1;
-      uint32_t tw[4], mw[4];
-      bits_b = chunk_step<R, QT>(tw, row, g.w(rb - 1), g.w(rb + 1), g.w(rb), k0, q, Rb, P.acc, mw);
-      if (ok && rb <= b1) store_words<4>(row + k0, tw);
-      if (!(ok && rb <= b1)) bits_b = 0;
-    }
-    if (COOP) {
-      warp_resolve<R>(g, scratch, bits_b, rb, pend, r - R, k0, P, tt);
-      if (pend)
-        *reinterpret_cast<uint4*>(out + PLANE + (size_t)(r - R) * H + k0) =
-            *reinterpret_cast<const uint4*>(g.w(r - R) + k0);
-    } else if (bits_b) {
-      own_resolve<R>(g, 0u, rb, k0, bits_b, P, tt);
+      const int r = b0 + s * R + 1 + tid / CPR;
+      if (ok && r <= b1) black_chunk<R>(g, r, tid % CPR, P, tt);
     }
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicOr(status, 1);
@@ -302,40 +190,37 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     if (tid < 32 && s + kAhead - 1 < nsteps) issue_stage<R>(g, s + kAhead - 1, b1, in, bar, tid);
     // ---- colour 1, rows b0+sR .. b0+(s+1)R-1 (<= b1-1); both colours of the row are stored
-    if (!PIPE) Rw = stream_block(P.key, P.rep, P_SWEEP_HI, 1u, (uint32_t)(r & (L - 1)), (uint32_t)c, tt);
-    {
+    const int r = b0 + s * R + tid / CPR, c = tid % CPR;
+    if (r <= b1 - 1) {
+      const int k0 = c * 16;
       uint8_t* row = g.w(r);
+      const uint8_t* mid = g.b(r);
+      const uint8_t* up = g.b(r - 1);
+      const uint8_t* dn = g.b(r + 1);
+      uint32_t tw[4], uw[4], dw[4], mw[4];
+      load_words4(row + k0, tw);
+      load_words4(up + k0, uw);
+      load_words4(dn + k0, dw);
+      load_words4(mid + k0, mw);
+      const uint32_t prv = load_word(mid + ((k0 - 4) & (H - 1))), nxt = load_word(mid + ((k0 + 16) & (H - 1)));
+      *reinterpret_cast<uint4*>(out + (size_t)r * H + k0) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+      const uint4 Rn = stream_block(P.key, P.rep, P_SWEEP_HI, 1u, (uint32_t)r, (uint32_t)c, tt);
       const int q = (r + 1) & 1;
-      uint32_t tw[4], mw[4];
-      uint32_t bits = chunk_step<R, QT>(tw, row, g.b(r - 1), g.b(r + 1), g.b(r), k0, q, Rw, P.acc, mw);
-      if (r <= b1 - 1) {
-        *reinterpret_cast<uint4*>(out + (size_t)r * H + k0) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
-        if (bits) {
-          store_words<4>(row + k0, tw);
-          if (!COOP) {
-            own_resolve<R>(g, 1u, r, k0, bits, P, tt);
-            load_words4(row + k0, tw);
-          }
+      uint32_t bits = update_chunk<4>(tw, uw, dw, mw, prv, nxt, (uint32_t)q, Rn, P.acc);
+      if (bits) {
+        store_words<4>(row + k0, tw);
+        while (bits) {
+          const int p = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const int k = k0 + open_byte(p);
+          if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], P.key, P.rep,
+                           1u, r, k, tt, P.acc))
+            row[k] ^= 1u;
         }
-        if (!COOP || !bits)
-          *reinterpret_cast<uint4*>(out + PLANE + (size_t)r * H + k0) = make_uint4(tw[0], tw[1], tw[2], tw[3]);
-      } else {
-        bits = 0;
+        load_words4(row + k0, tw);
       }
-      pend = COOP ? bits : 0u;
+      *reinterpret_cast<uint4*>(out + PLANE + (size_t)r * H + k0) = make_uint4(tw[0], tw[1], tw[2], tw[3]);
     }
-    if (PIPE) {
-      Rb = Rb_next;
-      Rw = Rw_next;
-    }
-  }
-  if (COOP) {
-    // ---- the last step's open colour-1 sites
-    const int rlast = b0 + (nsteps - 1) * R + rr;
-    warp_resolve<R>(g, scratch, 0u, rlast, pend, rlast, k0, P, tt);
-    if (pend)
-      *reinterpret_cast<uint4*>(out + PLANE + (size_t)rlast * H + k0) =
-          *reinterpret_cast<const uint4*>(g.w(rlast) + k0);
   }
 }
 

@@ -27,7 +27,6 @@
 
 #include "mcrg_ops.cuh"
 #include "mcrg_sweep_stream.cuh"
-#include "mcrg_sweep_stream_v1.cuh"
 #include "mcrg_sweep_tiled.cuh"
 #include "mcrg_tiled.cuh"
 
@@ -151,19 +150,15 @@ struct Variant {
 
 #define TILE_VARIANT(TR_, TC_) \
   Variant { "tiles", TR_, TC_, (const void*)tiled::sweep_kernel<TR_, TC_, 256>, tiled::sweep_smem_bytes<TR_, TC_>() }
-// stream variants are tagged TC = -(1 + mode), mode = PIPE + 2*COOP + 4*QT
-#define STREAM_VARIANT(R_, PIPE_, COOP_, QT_)                                                               \
-  Variant { "stream", R_, -(1 + PIPE_ + 2 * COOP_ + 4 * QT_),                                             \
-            (const void*)stream::sweep_kernel<R_, PIPE_, COOP_, QT_>, stream::smem_bytes<R_>() }
+// stream variants are tagged TC = -1 (TR = R rows per step)
+#define STREAM_VARIANT(R_) \
+  Variant { "stream", R_, -1, (const void*)stream::sweep_kernel<R_>, stream::smem_bytes<R_>() }
 
-const Variant kVariants[] = {TILE_VARIANT(32, 1024),        TILE_VARIANT(16, 1024),        TILE_VARIANT(32, 512),
-                             TILE_VARIANT(64, 512),         TILE_VARIANT(16, 512),         TILE_VARIANT(32, 256),
-                             TILE_VARIANT(16, 2048),        STREAM_VARIANT(1, 0, 1, 0),    STREAM_VARIANT(1, 0, 0, 0),
-                             STREAM_VARIANT(1, 0, 1, 1),    STREAM_VARIANT(1, 1, 1, 0),    STREAM_VARIANT(2, 0, 1, 0),
-                             STREAM_VARIANT(4, 0, 1, 0),    STREAM_VARIANT(8, 0, 1, 0),    STREAM_VARIANT(16, 0, 1, 0),
-                             STREAM_VARIANT(32, 0, 1, 0),
-                             Variant{"stream", 1, -100, (const void*)stream_v1::sweep_kernel<1>,
-                                     stream_v1::smem_bytes<1>()}};
+const Variant kVariants[] = {TILE_VARIANT(32, 1024), TILE_VARIANT(16, 1024), TILE_VARIANT(32, 512),
+                             TILE_VARIANT(64, 512),  TILE_VARIANT(16, 512),  TILE_VARIANT(32, 256),
+                             TILE_VARIANT(16, 2048), STREAM_VARIANT(1),      STREAM_VARIANT(2),
+                             STREAM_VARIANT(4),      STREAM_VARIANT(8),      STREAM_VARIANT(16),
+                             STREAM_VARIANT(32)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 bool variant_fits(const Variant& v, int L) {
@@ -181,18 +176,6 @@ int ctas_for(const Variant& v, int work_items, int threads) {
 
 void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
   const Variant& v = kVariants[vi];
-  if (v.TC == -100) {
-    stream_v1::Params P;
-    memset(&P, 0, sizeof P);
-    P.key = t->key;
-    P.rep = t->replica;
-    P.acc = t->acc;
-    int bands = t->L / (8 * v.TR);
-    if (bands > g_num_sms) bands = g_num_sms;
-    void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-    cudaLaunchKernel(v.kern, dim3(bands), dim3(stream_v1::kThreads), args, v.smem, s);
-    return;
-  }
   if (v.TC < 0) {
     stream::Params P;
     memset(&P, 0, sizeof P);
@@ -293,15 +276,7 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   cudaGetDevice(&dev);
   if (const char* force = getenv("MCRG_TILE")) {
     int tr = 0, tc = 0;
-    if (force[0] == 's') {
-      int mode = 2;  // cooperative resolution, selects
-      if (sscanf(force + 1, "%d.%d", &tr, &mode) < 1) tr = 0;
-      tc = -(1 + mode);
-    }
-    if (force[0] == 'v') {  // the earlier stream form
-      tr = 1;
-      tc = -100;
-    }
+    if (force[0] == 's' && sscanf(force + 1, "%d", &tr) == 1) tc = -1;
     if (force[0] == 's' || sscanf(force, "%dx%d", &tr, &tc) == 2)
       for (int v = 0; v < kNumVariants; ++v)
         if (kVariants[v].TR == tr && kVariants[v].TC == tc && variant_fits(kVariants[v], t->L)) return v;
