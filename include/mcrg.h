@@ -167,6 +167,25 @@ int mcrg_block_lattice(int32_t N, const int8_t* host_in, const int8_t* tie_value
 int mcrg_lattice_couplings(int32_t N, const int8_t* host_in, int32_t n_couplings, int64_t* out,
                            int32_t device);
 
+/* Same result as mcrg_lattice_couplings, for callers that must not allocate
+ * device memory while they run (a program that has given the rest of the GPU
+ * to its own memory pool or works under a fixed budget, where a cudaMalloc
+ * can fail, or one that cannot accept the device-wide synchronisation that
+ * cudaMalloc / cudaFree may cause).  It allocates nothing: the device-side
+ * working copy lives in a fixed scratch array that is part of libmcrg.so and
+ * stays reserved on every GPU that loads the library until the process ends
+ * (2 * MCRG_NOALLOC_MAX_L^2 + 256 bytes).  N above MCRG_NOALLOC_MAX_L is
+ * rejected with MCRG_ENOSPC.  The first call on a device looks the array's
+ * address up for that device; make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's data; the
+ * sums are cleared at the start of each call.  Calls on one device are
+ * serialised by a lock inside the library; device work that overlaps with a
+ * call in any other way races on the array.  No counterpart in the
+ * reference. */
+#define MCRG_NOALLOC_MAX_L 1024
+int mcrg_lattice_couplings_noalloc(int32_t N, const int8_t* host_in, int32_t n_couplings, int64_t* out,
+                                   int32_t device);
+
 /* ---------------------------------------------------------------------- */
 /* Batched solves: many independent chains (the reference runs one chain   */
 /* per MPI rank and sums with MPI_Allreduce, src/mcrg.cpp:101-103).         */

@@ -12,6 +12,7 @@ MAX_LEVELS = 14
 MAX_COUPLINGS = 5
 MAX_L = 16384
 SMEM_MAX_L = 256
+NOALLOC_MAX_L = 1024
 
 OK = 0
 ENOENT = -2
@@ -82,6 +83,7 @@ _SIGS = {
     "mcrg_block_lattice": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int32,
                                      C.c_uint32, C.c_void_p, C.c_int32]),
     "mcrg_lattice_couplings": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, P(C.c_int64), C.c_int32]),
+    "mcrg_lattice_couplings_noalloc": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, P(C.c_int64), C.c_int32]),
     "mcrg_batch_run": (C.c_int, [P(Request), C.c_int32, P(Result), C.c_int32, C.c_int32]),
     "mcrg_server_create": (C.c_int, [P(C.c_void_p), P(ServerCfg)]),
     "mcrg_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_uint64)]),
