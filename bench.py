@@ -141,11 +141,11 @@ def peaks() -> tuple[float, str]:
 
 def profiled_traffic(name: str):
     """Per-launch DRAM bytes of a kernel from a committed ncu summary line
-    'traffic_bytes_per_launch <kernel> <workload> <bytes>' in profiles/*.txt."""
+    'traffic_bytes_per_launch <kernel> <workload> <bytes>' in profiles/."""
     d = os.path.join(ROOT, "profiles")
     try:
         for fn in sorted(os.listdir(d)):
-            if not fn.endswith(".txt"):
+            if not fn.endswith((".txt", ".md")):
                 continue
             for ln in open(os.path.join(d, fn)):
                 f = ln.split()
@@ -204,8 +204,9 @@ def run_large(args, D: Dist) -> dict:
     alg_bytes = 2.0 * L * L  # one read + one write of every int8 site
     peak, kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
-    traffic = profiled_traffic("tiled_sweep_kernel")
     tile = lat.tile_shape()
+    kname = "stream_sweep" if tile and tile[1] == -1 else ("stream2_sweep" if tile and tile[1] < -1 else "tiles_sweep")
+    traffic = profiled_traffic(kname)
 
     # ---- end to end through the C ABI with host buffers
     hspins = torch.empty((L, L), dtype=torch.int8, pin_memory=True)
@@ -241,7 +242,7 @@ def run_large(args, D: Dist) -> dict:
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": "tiled sweep_kernel", "tile": tile, "peak_kind": kind,
+                     "kernel": kname, "tile": tile, "peak_kind": kind,
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(sweep_ms, 4)},
         "clocks": clocks,
         "moments_samples": tot.n_samples,
@@ -388,40 +389,70 @@ def run_served(args, D: Dist) -> dict:
 # ---------------------------------------------------------------------------
 # reference arm: the reference's CPU path (restated), all host threads
 # ---------------------------------------------------------------------------
-def cpu_reference(L: int, seconds: float, threads: int, n_couplings: int = 2) -> dict:
+class RefCPU:
     """The reference's sample loop (src/mcrg.cpp:72-98: one Wolff update, then
-    coupling sums + blocking at every level) on `threads` independent replicas,
-    each on its own OS thread, for about `seconds`."""
-    from oracle import oracle as O
-    nl = int(math.log2(L)) - 1
-    res = [None] * threads
+    coupling sums + blocking at every level) on `threads` independent
+    replicas, each on its own OS thread (the oracle's restatement; ctypes
+    releases the GIL).  Replicas start ordered and are relaxed once."""
 
-    def work(k):
-        s = O.init_spins(L, 1000 + k)
-        s[:] = 1  # ordered start: Wolff relaxes from it in a few steps at K = Kc
-        w = O.Wolff(L, KC, 1000 + k)
-        w.steps(s, 3)
+    def __init__(self, L: int, threads: int, n_couplings: int = 2, relax_steps: int = 3):
+        from oracle import oracle as O
+        self.O = O
+        self.L, self.threads, self.C = L, threads, n_couplings
+        self.nl = int(math.log2(L)) - 1
+        self.spins = [None] * threads
+        self.wolff = [None] * threads
+        self.samples = [0] * threads
+
+        def init(k):
+            s = np.empty((L, L), dtype=np.int8)
+            s[:] = 1  # ordered start: Wolff relaxes from it in a few steps at K = Kc
+            w = O.Wolff(L, KC, 1000 + k)
+            w.steps(s, relax_steps)
+            self.spins[k], self.wolff[k] = s, w
+
+        import numpy as np
+        self._run(init)
+
+    def _run(self, fn):
+        ths = [threading.Thread(target=fn, args=(k,)) for k in range(self.threads)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    def step(self, seconds: float) -> dict:
+        res = [None] * self.threads
+
+        def work(k):
+            t0 = time.perf_counter()
+            flipped = n = 0
+            while True:
+                flipped += self.wolff[k].steps(self.spins[k], 1)
+                self.O.measure(self.spins[k], self.C, self.nl, 1000 + k, 0, self.samples[k])
+                self.samples[k] += 1
+                n += 1
+                if time.perf_counter() - t0 > seconds:
+                    break
+            res[k] = (flipped, n)
+
         t0 = time.perf_counter()
-        flipped = samples = 0
-        while True:
-            flipped += w.steps(s, 1)
-            O.measure(s, n_couplings, nl, 1000 + k, 0, samples)
-            samples += 1
-            if time.perf_counter() - t0 > seconds:
-                break
-        w.close()
-        res[k] = (flipped, samples, time.perf_counter() - t0)
+        self._run(work)
+        wall = time.perf_counter() - t0
+        return {"flips_per_s": sum(r[0] for r in res) / wall, "samples": sum(r[1] for r in res), "wall_s": wall}
 
-    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
-    t0 = time.perf_counter()
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
-    wall = time.perf_counter() - t0
-    flipped = sum(r[0] for r in res)
-    samples = sum(r[1] for r in res)
-    return {"flips_per_s": flipped / wall, "samples": samples, "wall_s": wall}
+    def close(self):
+        for w in self.wolff:
+            if w is not None:
+                w.close()
+
+
+def cpu_reference(L: int, seconds: float, threads: int, n_couplings: int = 2) -> dict:
+    ref = RefCPU(L, threads, n_couplings)
+    try:
+        return ref.step(seconds)
+    finally:
+        ref.close()
 
 
 def cpu_threads(L: int) -> int:
@@ -460,11 +491,13 @@ def main():
             return
         threads = cpu_threads(args.L)
         per = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+        ref = RefCPU(args.L, threads)
         vals = []
         for _ in range(args.warmup):
-            cpu_reference(args.L, per / 2, threads)
+            ref.step(per / 2)
         for _ in range(args.steps):
-            vals.append(cpu_reference(args.L, per, threads))
+            vals.append(ref.step(per))
+        ref.close()
         fl = sum(v["flips_per_s"] for v in vals) / len(vals) / 1e9
         out = {"impl": "reference", "metric": "Gflips/s", "value": round(fl, 4), "unit": "Gflips/s",
                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,

@@ -21,7 +21,7 @@
 namespace mcrg {
 
 // One sweep of a resident lattice: colour 0, then colour 1.
-__device__ __noinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key key, uint32_t rep, const Accept& acc,
+__device__ __forceinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key key, uint32_t rep, const Accept& acc,
                                          bool vec, int tid, int T, uint32_t* scratch) {
   for (int c = 0; c < 2; ++c) {
     if (vec) {

@@ -100,6 +100,11 @@ __device__ __forceinline__ bool resolve_open(uint32_t t, uint32_t n0, uint32_t n
 
 // Descriptors one warp resolves cooperatively per pass (scratch entries).
 constexpr int kOpenPerWarp = 64;
+// Resident sweeps resolve open sites warp-cooperatively (true) or per thread.
+#ifndef MCRG_RESIDENT_WARP_RESOLVE
+#define MCRG_RESIDENT_WARP_RESOLVE 0
+#endif
+constexpr bool kResolveInWarp = MCRG_RESIDENT_WARP_RESOLVE != 0;
 
 // Resolves the open sites of the warp's chunks of one round.  om[r] is the
 // open mask of this lane's chunk r (row i_r, first byte k_r).  The sites are
@@ -189,7 +194,30 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
         store_words<NW>(tp, tw);
       }
     }
-    warp_resolve_resident<NW>(lat, n, c, t, key, rep, a, om, base, tid, T, cpr, scratch);
+    if (kResolveInWarp) {
+      warp_resolve_resident<NW>(lat, n, c, t, key, rep, a, om, base, tid, T, cpr, scratch);
+    } else {
+      // each thread resolves the open sites of its own chunks (inline: a call
+      // would make every warp save and restore its registers)
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        uint32_t bits = om[r];
+        if (!bits) continue;
+        const int task = base + tid + r * T;
+        const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB, q = (i + c) & 1;
+        const uint8_t* orow = Oc + (size_t)i * half;
+        while (bits) {
+          const int p = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const int k = k0 + open_byte(p);
+          uint8_t* sp = Cc + (size_t)i * half + k;
+          if (resolve_open(*sp, Oc[(size_t)((i - 1) & (n - 1)) * half + k],
+                           Oc[(size_t)((i + 1) & (n - 1)) * half + k], orow[(k - 1 + q) & (half - 1)],
+                           orow[(k + q) & (half - 1)], key, rep, (uint32_t)c, i, k, t, a))
+            *sp ^= 1u;
+        }
+      }
+    }
   }
 }
 

@@ -226,3 +226,221 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace stream
 }  // namespace mcrg
+
+// ===========================================================================
+// Two-CTA-per-SM form for one row per step: NT threads, each updating CH =
+// CPR / NT chunks of each colour per step in one straight-line block (CH
+// independent Philox chains give the scheduler instruction-level
+// parallelism), a ring of SL slots per colour (modulo indexing) so that two
+// CTAs fit one SM and one CTA's barrier is covered by the other's work.
+// Prefetch: the stage of step s + SL - 4 is issued after step s's barrier.
+// ===========================================================================
+namespace mcrg {
+namespace stream2 {
+
+using stream::Params;
+
+template <int CPR, int NT, int SL>
+struct Geo {
+  static constexpr int CH = CPR / NT;
+  static constexpr int H = CPR * 16;
+  static constexpr int L = 2 * H;
+  static constexpr int AHEAD = SL - 4;  // stages issued ahead (prologue stage + AHEAD)
+};
+
+template <int CPR, int NT, int SL>
+constexpr size_t smem_bytes() {
+  return 128 + 2 * (size_t)SL * (size_t)CPR * 16;
+}
+
+template <int SL>
+__device__ __forceinline__ int slot_of(int r, int b0) {
+  return (r - b0 + 2) % SL;
+}
+
+template <int CPR, int NT, int SL>
+__global__ void __launch_bounds__(NT, 2)
+    sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, Params P, uint32_t tt,
+                 int* __restrict__ status) {
+  using G = Geo<CPR, NT, SL>;
+  constexpr int H = G::H, L = G::L, CH = G::CH;
+  constexpr size_t PLANE = (size_t)L * H;
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  uint8_t* Ws = smem + 128;
+  uint8_t* Bs = Ws + SL * H;
+  const int tid = threadIdx.x;
+  const int b0 = (int)(((long long)blockIdx.x * L) / gridDim.x);
+  const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
+  const int nsteps = b1 - b0;
+  const Key key = P.key;
+  const uint32_t rep = P.rep;
+  auto W = [&](int r) { return Ws + slot_of<SL>(r, b0) * H; };
+  auto B = [&](int r) { return Bs + slot_of<SL>(r, b0) * H; };
+
+  // stage k >= 0: colour-1 row b0+k+2 (<= b1+1) and colour-0 row b0+k+1 (<= b1);
+  // stage -1: colour-1 rows b0-2 .. b0+1, colour-0 rows b0-1, b0
+  auto issue = [&](int k) {
+    int w_lo, w_hi, b_lo, b_hi;
+    if (k < 0) {
+      w_lo = b0 - 2; w_hi = b0 + 1; b_lo = b0 - 1; b_hi = b0;
+    } else {
+      w_lo = b0 + k + 2; w_hi = min(b0 + k + 2, b1 + 1);
+      b_lo = b0 + k + 1; b_hi = min(b0 + k + 1, b1);
+    }
+    const int nw = max(0, w_hi - w_lo + 1), nb = max(0, b_hi - b_lo + 1);
+    uint64_t* br = &bar[(k + 1) & (stream::kStages - 1)];
+    if (tid == 0) {
+      stream::fence_proxy_async();
+      stream::mbar_expect_tx(br, (uint32_t)((nw + nb) * H));
+    }
+    __syncwarp();
+    for (int x = tid; x < nw + nb; x += 32) {
+      if (x < nw) {
+        const int r = w_lo + x;
+        stream::bulk_g2s(W(r), in + PLANE + (size_t)((r + L) & (L - 1)) * H, H, br);
+      } else {
+        const int r = b_lo + x - nw;
+        stream::bulk_g2s(B(r), in + (size_t)((r + L) & (L - 1)) * H, H, br);
+      }
+    }
+  };
+
+  // CH chunks of colour `colour` of row r, chunks tid + h*NT; tp = own-colour row,
+  // up/dn/mid = other-colour rows r-1, r+1, r.  Returns nothing; stores in place
+  // (colour 0) and optionally to `gout` (colour 1).
+  if (tid < stream::kStages) stream::mbar_init(&bar[tid], 1);
+  if (tid == 0) stream::fence_mbar_init();
+  __syncthreads();
+  if (tid < 32)
+    for (int k = -1; k < G::AHEAD && k < nsteps; ++k) issue(k);
+
+  bool ok = stream::wait_stage(bar, -1);
+  // ---- prologue: colour 0 on rows b0-1, b0
+  for (int pr = 0; pr < 2; ++pr) {
+    const int r = b0 - 1 + pr;
+    const int gr = (r + L) & (L - 1), q = gr & 1;
+    uint8_t* row = B(r);
+    const uint8_t* mid = W(r);
+    const uint8_t* up = W(r - 1);
+    const uint8_t* dn = W(r + 1);
+    uint32_t bits[CH];
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      const int c = tid + h * NT, k0 = c * 16;
+      uint32_t tw[4], uw[4], dw[4], mw[4];
+      load_words4(row + k0, tw);
+      load_words4(up + k0, uw);
+      load_words4(dn + k0, dw);
+      load_words4(mid + k0, mw);
+      const uint4 Rn = stream_block(key, rep, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)c, tt);
+      bits[h] = update_chunk<4>(tw, uw, dw, mw, load_word(mid + ((k0 - 4) & (H - 1))),
+                                load_word(mid + ((k0 + 16) & (H - 1))), (uint32_t)q, Rn, P.acc);
+      if (ok) store_words<4>(row + k0, tw);
+    }
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      uint32_t b = ok ? bits[h] : 0u;
+      const int k0 = (tid + h * NT) * 16;
+      while (b) {
+        const int p = __ffs(b) - 1;
+        b &= b - 1;
+        const int k = k0 + open_byte(p);
+        if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], key, rep, 0u, gr,
+                         k, tt, P.acc))
+          row[k] ^= 1u;
+      }
+    }
+  }
+
+  for (int s = 0; s < nsteps; ++s) {
+    if (!stream::wait_stage(bar, s)) ok = false;
+    // ---- colour 0, row rb = b0+s+1 (<= b1)
+    {
+      const int rb = b0 + s + 1;
+      const int gr = (rb + L) & (L - 1), q = gr & 1;
+      uint8_t* row = B(rb);
+      const uint8_t* mid = W(rb);
+      const uint8_t* up = W(rb - 1);
+      const uint8_t* dn = W(rb + 1);
+      uint32_t bits[CH];
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        const int c = tid + h * NT, k0 = c * 16;
+        uint32_t tw[4], uw[4], dw[4], mw[4];
+        load_words4(row + k0, tw);
+        load_words4(up + k0, uw);
+        load_words4(dn + k0, dw);
+        load_words4(mid + k0, mw);
+        const uint4 Rn = stream_block(key, rep, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)c, tt);
+        bits[h] = update_chunk<4>(tw, uw, dw, mw, load_word(mid + ((k0 - 4) & (H - 1))),
+                                  load_word(mid + ((k0 + 16) & (H - 1))), (uint32_t)q, Rn, P.acc);
+        if (ok) store_words<4>(row + k0, tw);
+      }
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        uint32_t b = ok ? bits[h] : 0u;
+        const int k0 = (tid + h * NT) * 16;
+        while (b) {
+          const int p = __ffs(b) - 1;
+          b &= b - 1;
+          const int k = k0 + open_byte(p);
+          if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], key, rep, 0u,
+                           gr, k, tt, P.acc))
+            row[k] ^= 1u;
+        }
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(status, 1);
+      return;
+    }
+    if (tid < 32 && s + G::AHEAD < nsteps) issue(s + G::AHEAD);
+    // ---- colour 1, row r = b0+s; both colours of the row are stored
+    {
+      const int r = b0 + s;
+      const int q = (r + 1) & 1;
+      uint8_t* row = W(r);
+      const uint8_t* mid = B(r);
+      const uint8_t* up = B(r - 1);
+      const uint8_t* dn = B(r + 1);
+      uint32_t bits[CH];
+      uint32_t keep[CH][4];
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        const int c = tid + h * NT, k0 = c * 16;
+        uint32_t uw[4], dw[4], mw[4];
+        load_words4(row + k0, keep[h]);
+        load_words4(up + k0, uw);
+        load_words4(dn + k0, dw);
+        load_words4(mid + k0, mw);
+        *reinterpret_cast<uint4*>(out + (size_t)r * H + k0) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+        const uint4 Rn = stream_block(key, rep, P_SWEEP_HI, 1u, (uint32_t)r, (uint32_t)c, tt);
+        bits[h] = update_chunk<4>(keep[h], uw, dw, mw, load_word(mid + ((k0 - 4) & (H - 1))),
+                                  load_word(mid + ((k0 + 16) & (H - 1))), (uint32_t)q, Rn, P.acc);
+      }
+#pragma unroll
+      for (int h = 0; h < CH; ++h) {
+        const int k0 = (tid + h * NT) * 16;
+        uint32_t b = bits[h];
+        if (b) {
+          store_words<4>(row + k0, keep[h]);
+          while (b) {
+            const int p = __ffs(b) - 1;
+            b &= b - 1;
+            const int k = k0 + open_byte(p);
+            if (resolve_open(row[k], up[k], dn[k], mid[(k - 1 + q) & (H - 1)], mid[(k + q) & (H - 1)], key, rep, 1u,
+                             r, k, tt, P.acc))
+              row[k] ^= 1u;
+          }
+          load_words4(row + k0, keep[h]);
+        }
+        *reinterpret_cast<uint4*>(out + PLANE + (size_t)r * H + k0) =
+            make_uint4(keep[h][0], keep[h][1], keep[h][2], keep[h][3]);
+      }
+    }
+  }
+}
+
+}  // namespace stream2
+}  // namespace mcrg

@@ -154,14 +154,30 @@ struct Variant {
 #define STREAM_VARIANT(R_) \
   Variant { "stream", R_, -1, (const void*)stream::sweep_kernel<R_>, stream::smem_bytes<R_>() }
 
+// two-CTA streaming variants: TC = -(2 + index), TR = 1 (one row per step)
+#define STREAM2_VARIANT(CPR_, NT_, SL_, TAG_)                                                            \
+  Variant { "stream2", 1, -(2 + TAG_), (const void*)stream2::sweep_kernel<CPR_, NT_, SL_>,             \
+            stream2::smem_bytes<CPR_, NT_, SL_>() }
+
 const Variant kVariants[] = {TILE_VARIANT(32, 1024), TILE_VARIANT(16, 1024), TILE_VARIANT(32, 512),
                              TILE_VARIANT(64, 512),  TILE_VARIANT(16, 512),  TILE_VARIANT(32, 256),
                              TILE_VARIANT(16, 2048), STREAM_VARIANT(1),      STREAM_VARIANT(2),
                              STREAM_VARIANT(4),      STREAM_VARIANT(8),      STREAM_VARIANT(16),
-                             STREAM_VARIANT(32)};
+                             STREAM_VARIANT(32),     STREAM2_VARIANT(512, 256, 7, 0),
+                             STREAM2_VARIANT(512, 128, 7, 1), STREAM2_VARIANT(256, 256, 7, 2),
+                             STREAM2_VARIANT(256, 128, 7, 3)};
+// L of a two-CTA streaming variant
+int stream2_L(const Variant& v) {
+  switch (-v.TC - 2) {
+    case 0: case 1: return 16384;
+    default: return 8192;
+  }
+}
+int stream2_threads(const Variant& v) { return (-v.TC - 2) & 1 ? 128 : 256; }
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 bool variant_fits(const Variant& v, int L) {
+  if (v.TC < -1) return L == stream2_L(v);
   if (v.TC < 0) return L * v.TR == 16384;
   return (L / 2) % v.TC == 0 && L % v.TR == 0;
 }
@@ -176,6 +192,19 @@ int ctas_for(const Variant& v, int work_items, int threads) {
 
 void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
   const Variant& v = kVariants[vi];
+  if (v.TC < -1) {
+    stream::Params P;
+    memset(&P, 0, sizeof P);
+    P.key = t->key;
+    P.rep = t->replica;
+    P.acc = t->acc;
+    // bands of at least 16 rows, up to two CTAs per SM
+    int bands = t->L / 16;
+    if (bands > 2 * g_num_sms) bands = 2 * g_num_sms;
+    void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
+    cudaLaunchKernel(v.kern, dim3(bands), dim3(stream2_threads(v)), args, v.smem, s);
+    return;
+  }
   if (v.TC < 0) {
     stream::Params P;
     memset(&P, 0, sizeof P);
@@ -277,7 +306,11 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   if (const char* force = getenv("MCRG_TILE")) {
     int tr = 0, tc = 0;
     if (force[0] == 's' && sscanf(force + 1, "%d", &tr) == 1) tc = -1;
-    if (force[0] == 's' || sscanf(force, "%dx%d", &tr, &tc) == 2)
+    if (force[0] == 't' && sscanf(force + 1, "%d", &tc) == 1) {  // two-CTA streaming variant t<index>
+      tr = 1;
+      tc = -(2 + tc);
+    }
+    if (force[0] == 's' || force[0] == 't' || sscanf(force, "%dx%d", &tr, &tc) == 2)
       for (int v = 0; v < kNumVariants; ++v)
         if (kVariants[v].TR == tr && kVariants[v].TC == tc && variant_fits(kVariants[v], t->L)) return v;
   }

@@ -312,10 +312,12 @@ def _variants_for(N):
     out = ["%dx%d" % (tr, tc) for tr, tc in tiles if (N // 2) % tc == 0 and N % tr == 0]
     if 16384 % N == 0:
         out.append("s%d" % (16384 // N))
+    if N == 8192:
+        out += ["t2", "t3"]
     return out
 
 
-@pytest.mark.parametrize("N", [512, 1024, 2048, 4096])
+@pytest.mark.parametrize("N", [512, 1024, 2048, 4096, 8192])
 def test_every_sweep_variant_bit_exact(M, N, monkeypatch):
     init = O.init_spins(N, 77, 4)
     ref = O.sweep(init, KC, 77, 4, 0, 2)
@@ -336,7 +338,7 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
     init = O.init_spins(N, 5, 0)
     ref = O.sweep(init, KC, 5, 0, 0, 1)
     ref_S = O.couplings(ref, 5)
-    for v in ("s1", "32x1024"):
+    for v in ("s1", "t0", "t1", "32x1024"):
         monkeypatch.setenv("MCRG_TILE", v)
         lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
         lat.sweep(1)
