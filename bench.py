@@ -205,7 +205,7 @@ def run_large(args, D: Dist) -> dict:
     peak, kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
     tile = lat.tile_shape()
-    kname = "stream_sweep" if tile and tile[1] == -1 else ("stream2_sweep" if tile and tile[1] < -1 else "tiles_sweep")
+    kname = "bits_sweep_b%d" % tile[1]
     traffic = profiled_traffic(kname)
 
     # ---- end to end through the C ABI with host buffers
@@ -242,7 +242,7 @@ def run_large(args, D: Dist) -> dict:
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "kernel": kname, "tile": tile, "peak_kind": kind,
+                     "kernel": kname, "rows_threads": tile, "peak_kind": kind,
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(sweep_ms, 4)},
         "clocks": clocks,
         "moments_samples": tot.n_samples,

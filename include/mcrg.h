@@ -28,9 +28,13 @@
  * (row, purpose<<28 | sub<<20 | group, time, replica):
  *   init   purpose 1, sub = colour, group = k>>7, time 0:
  *          spin bit = bit (k&127) of the 128-bit block;
- *   sweep  purpose 2, sub = colour, group = k>>4, time = sweep index t:
- *          r8 = byte (k&15); purpose 3, group = k>>2: r24 = low 24 bits of
- *          word (k&3); u32 = r8<<24 | r24;
+ *   sweep  purpose 2, sub = colour, time = sweep index t; the 8-bit draw r8:
+ *          L <= MCRG_SMEM_MAX_L: group = k>>4, r8 = byte (k&15);
+ *          L >  MCRG_SMEM_MAX_L: groups 2w, 2w+1 with w = k>>5 give eight
+ *            plane words W0..W7; bit 7-q of r8 is bit 8*(p&3)+(p>>2) of Wq,
+ *            p = k&31;
+ *          purpose 3, group = k>>2: r24 = low 24 bits of word (k&3);
+ *          u32 = r8<<24 | r24;
  *   ties   purpose 4, sub = level produced, row = ib, group = jb>>7,
  *          time = sample index: tie value = bit (jb&127) ? +1 : -1.
  * Site (i, j) has colour c = (i+j)&1 and split index k = j>>1.  Colour 0 is
@@ -150,9 +154,10 @@ int mcrg_measure(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_
 
 /* Sweep and sample counters (the Philox time words of the next sweep / sample). */
 int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);
-/* Tile shape the autotuner picked for an HBM-tiled context (rows x bytes per
- * colour row); MCRG_EINVAL for shared-memory-resident contexts and
- * MCRG_EAGAIN before the first sweep.  No counterpart in the reference. */
+/* Sweep schedule the autotuner picked for an HBM-resident context: rows per
+ * pipeline group (tile_rows) and threads per CTA (tile_cols); MCRG_EINVAL
+ * for shared-memory-resident contexts and MCRG_EAGAIN before the first
+ * sweep.  No counterpart in the reference. */
 int mcrg_tile_shape(mcrg_ctx* ctx, int32_t* tile_rows, int32_t* tile_cols);
 /* The context's CUDA stream (cudaStream_t), for event timing. */
 int mcrg_stream(mcrg_ctx* ctx, void** stream);

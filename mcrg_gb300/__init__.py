@@ -135,7 +135,8 @@ class Lattice:
         return int(t.value), int(n.value)
 
     def tile_shape(self):
-        """(rows, bytes) of the autotuned sweep tile, or None for resident lattices."""
+        """(rows per pipeline group, threads per CTA) of the autotuned HBM sweep,
+        or None for shared-memory-resident lattices."""
         r, c = C.c_int32(), C.c_int32()
         rc = lib().mcrg_tile_shape(self._ctx, C.byref(r), C.byref(c))
         return (r.value, c.value) if rc == 0 else None

@@ -1,0 +1,337 @@
+// mcrg_sweep_bits.cuh -- bit-sliced fused two-colour sweep of an HBM-resident
+// lattice (L = 512 .. 16384): one read and one write of every int8 site per
+// sweep, the update itself on 32 sites per 32-bit word.
+//
+// Bit-plane words.  32 consecutive sites k = 32w .. 32w+31 of one colour row
+// form plane word w; site k = 32w + p sits at bit pos(p) = 8*(p&3) + (p>>2).
+// That order makes packing 32 int8 sites (bytes 0/1) a sum of eight shifted
+// 32-bit loads and unpacking eight shift-and-mask pairs.  The update draws
+// eight random planes per word from two Philox blocks (row, P_SWEEP_HI,
+// colour, group 2w and 2w+1, sweep): bit pos(p) of plane q is bit 7-q of the
+// site's 8-bit draw r8.  For the fast acceptance regime (m >= 2 always flips,
+// m in {0,1} flips iff r8:r24 < thr[m]) the decision for all 32 sites is a
+// bit-sliced borrow chain r8 - T8[m] plus an equality mask; a site whose r8
+// equals T8[m] is "open" and is decided from the low 24 bits of its
+// P_SWEEP_LO draw exactly as the byte form does.
+//
+// Schedule.  Each CTA owns a band of rows [b0, b1) and walks it in groups of
+// R = NT / (L/64) rows (one plane word per thread per colour per group).  A
+// group g covers rows b0-2+gR .. b0-2+(g+1)R-1.  Phase p (one barrier each):
+//   - resolve the open sites queued by colour 0 of group p-3 (flip bits of
+//     the packed colour-0 rows in shared memory) and by colour 1 of group p-6
+//     (patch the bytes already written to HBM);
+//   - one warp issues the bulk copies of group p+LEAD (both colours);
+//   - pack group p from its landed byte rows into plane words;
+//   - update colour 0 of group p-2 (reads old colour-1 planes), queue its
+//     open sites;
+//   - update colour 1 of group p-5 (reads new colour-0 planes of groups p-6 ..
+//     p-4, all resolved), queue its open sites, and write both colours of its
+//     rows to the output buffer.
+// The lags make every read in a phase depend only on work that finished
+// before the previous barrier, so one barrier per phase suffices and the
+// rare open sites are resolved compactly by a few lanes instead of stalling
+// every warp that holds one.  Colour 0 is updated on rows b0-1 .. b1 and
+// colour 1 on b0 .. b1-1; halo rows are also updated by the neighbouring
+// band with the same draws, so both compute the same values.  Input and
+// output are the two buffers of a ping-pong pair.
+#pragma once
+#include "mcrg_ops.cuh"
+#include "mcrg_tma.cuh"
+
+namespace mcrg {
+namespace bits {
+
+struct Params {
+  uint32_t rep;
+  uint32_t thr0, thr1;  // acceptance thresholds for m = 0 and m = 1
+  uint32_t rk[20];      // Philox round keys: rk[2r] = k0 + r*W0, rk[2r+1] = k1 + r*W1
+  uint32_t tz[8], to[8];  // threshold top bytes as all-ones / all-zero masks, plane q (q = 0 MSB)
+};
+
+// Kernel parameters live in the constant bank, so the round keys and the
+// threshold masks enter the logic ops as constant operands instead of
+// occupying registers or being recomputed per Philox call.
+inline void fill_params(Params& P, Key key, uint32_t rep, uint32_t thr0, uint32_t thr1) {
+  P.rep = rep;
+  P.thr0 = thr0;
+  P.thr1 = thr1;
+  uint32_t k0 = key.k0, k1 = key.k1;
+  for (int r = 0; r < 10; ++r) {
+    P.rk[2 * r] = k0;
+    P.rk[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  const uint32_t T0 = thr0 >> 24, T1 = thr1 >> 24;
+  for (int q = 0; q < 8; ++q) {
+    P.tz[q] = 0u - ((T0 >> (7 - q)) & 1u);
+    P.to[q] = 0u - ((T1 >> (7 - q)) & 1u);
+  }
+}
+
+// Philox4x32-10 with precomputed round keys (same stream as philox10()).
+__device__ __forceinline__ uint4 draw(const Params& P, uint32_t purpose, uint32_t sub, uint32_t row, uint32_t group,
+                                      uint32_t tt) {
+  uint4 c = make_uint4(row, (purpose << 28) | (sub << 20) | group, tt, P.rep);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ P.rk[2 * r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ P.rk[2 * r + 1],
+                   (uint32_t)p0);
+  }
+  return c;
+}
+
+// Row groups of byte rows in flight ahead of packing: LEAD; LEAD + 1 are held
+// per colour.
+constexpr int kPackSlots = 8;          // plane-word groups held per colour
+constexpr int kQueueCap = 256;         // open sites per queue (more are resolved by their owner)
+
+template <int NT, int LEAD>
+constexpr size_t smem_bytes() {
+  return 128 + 6 * (size_t)kQueueCap * 4 + 2 * (size_t)(LEAD + 1) * NT * 32 + 2 * (size_t)kPackSlots * NT * 4;
+}
+
+// plane bit of site p (0..31) of a word, and its inverse
+__device__ __forceinline__ int plane_pos(int p) { return 8 * (p & 3) + (p >> 2); }
+__device__ __forceinline__ int plane_site(int pos) { return 4 * (pos & 7) + (pos >> 3); }
+
+// 32 sites (bytes 0/1, a = bytes 0..15, b = bytes 16..31) -> plane word
+__device__ __forceinline__ uint32_t pack_bytes(const uint4& a, const uint4& b) {
+  return a.x + (a.y << 1) + (a.z << 2) + (a.w << 3) + (b.x << 4) + (b.y << 5) + (b.z << 6) + (b.w << 7);
+}
+
+__device__ __forceinline__ void unpack_bytes(uint32_t x, uint4& a, uint4& b) {
+  const uint32_t M = 0x01010101u;
+  a = make_uint4(x & M, (x >> 1) & M, (x >> 2) & M, (x >> 3) & M);
+  b = make_uint4((x >> 4) & M, (x >> 5) & M, (x >> 6) & M, (x >> 7) & M);
+}
+
+// Word of the sites k+1 (right) / k-1 (left) of every site k of word x;
+// xn / xp is the next / previous word of the row.
+__device__ __forceinline__ uint32_t right_sites(uint32_t x, uint32_t xn) {
+  return (x >> 8) | ((x << 23) & 0x7F000000u) | (xn << 31);
+}
+__device__ __forceinline__ uint32_t left_sites(uint32_t x, uint32_t xp) {
+  return (x << 8) | ((x >> 23) & 0xFEu) | (xp >> 31);
+}
+
+// Bit-sliced update of 32 sites t from their neighbours u, d (other colour,
+// rows above and below), mid (same byte index) and side (the other
+// horizontal neighbour).  Returns the new word; `open` gets the sites whose
+// draw ties the threshold's top byte, `zero` the sites with m = 0.
+__device__ __forceinline__ uint32_t decide(uint32_t t, uint32_t u, uint32_t d, uint32_t mid, uint32_t side,
+                                           const uint4& A, const uint4& B, const Params& P, uint32_t& open,
+                                           uint32_t& zero) {
+  const uint32_t s1 = (u ^ t) | (d ^ t), p1 = (u ^ t) & (d ^ t);
+  const uint32_t s2 = (mid ^ t) | (side ^ t), p2 = (mid ^ t) & (side ^ t);
+  const uint32_t ge2 = p1 | p2 | (s1 & s2);  // m >= 2: always flips
+  zero = ~(s1 | s2);
+  const uint32_t W[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+  uint32_t br = 0u, eq = ~0u;  // borrow of r8 - T8 (r8 < T8), r8 == T8
+#pragma unroll
+  for (int q = 7; q >= 0; --q) {
+    const uint32_t th = (zero & P.tz[q]) | (~zero & P.to[q]);
+    br = (~W[q] & (th | br)) | (th & br);
+    eq &= ~(W[q] ^ th);
+  }
+  open = eq & ~ge2;
+  return t ^ (ge2 | br);
+}
+
+// Exact decision of one open site of colour c, row gr, byte k.
+__device__ __forceinline__ bool open_flips(const Params& P, uint32_t c, int gr, int k, uint32_t m, uint32_t tt) {
+  const uint4 lo = draw(P, P_SWEEP_LO, c, (uint32_t)gr, (uint32_t)(k >> 2), tt);
+  const uint32_t th = m ? P.thr1 : P.thr0;
+  return (u4get(lo, k & 3) & 0xFFFFFFu) < (th & 0xFFFFFFu);
+}
+
+// Queues the open sites of word w (row x, band offset off) of colour c;
+// returns the bits of those that did not fit and were resolved here.
+__device__ __forceinline__ uint32_t enqueue(uint32_t open, uint32_t zero, uint32_t t, int* qn, uint32_t* Q, int c,
+                                         int qi, int off, int w, int gr, const Params& P, uint32_t tt) {
+  int slot = atomicAdd(&qn[qi], __popc(open));
+  uint32_t* q = Q + qi * kQueueCap;
+  uint32_t flips = 0;
+  while (open) {
+    const int pos = __ffs(open) - 1;
+    open &= open - 1;
+    const int k = 32 * w + plane_site(pos);
+    const uint32_t m = ((zero >> pos) & 1u) ^ 1u;
+    if (slot < kQueueCap)
+      q[slot] = (uint32_t)k | (m << 14) | (((t >> pos) & 1u) << 15) | ((uint32_t)off << 16);
+    else if (open_flips(P, (uint32_t)c, gr, k, m, tt))
+      flips |= 1u << pos;
+    ++slot;
+  }
+  return flips;
+}
+
+// Geometry of one instantiation: lattice side L = 64 << LW, NT threads.
+template <int NT, int LW, int LEAD>
+struct Geo {
+  static constexpr int L = 64 << LW;
+  static constexpr int H = L / 2;              // bytes per colour row
+  static constexpr int WPR = 1 << LW;          // plane words per colour row
+  static constexpr int R = NT >> LW;           // rows per group
+  static constexpr int RAW_ROWS = (LEAD + 1) * R;
+  static constexpr int PK_ROWS = kPackSlots * R;
+  static constexpr size_t PLANE = (size_t)L * H;
+  static_assert(R >= 1, "one plane word per thread per group row");
+};
+
+template <int NT, int LW, int LEAD>
+__device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, const uint8_t* in, uint8_t* raw,
+                                            uint64_t* bar, int lane) {
+  using G = Geo<NT, LW, LEAD>;
+  const int x0 = top + g * G::R;
+  // rows wanted: colour 0 on [b0-1, b1], colour 1 on [b0-2, b1+1]
+  const int n0 = max(0, min(b1, x0 + G::R - 1) - max(b0 - 1, x0) + 1);
+  const int n1 = max(0, min(b1 + 1, x0 + G::R - 1) - max(b0 - 2, x0) + 1);
+  uint64_t* br = &bar[g % (LEAD + 1)];
+  tma::fence_proxy_async();
+  if (lane == 0) tma::mbar_expect_tx(br, (uint32_t)((n0 + n1) * G::H));
+  __syncwarp();
+  for (int e = lane; e < 2 * G::R; e += 32) {
+    const int c = e >= G::R, x = x0 + (e - c * G::R);
+    const bool want = c ? (x >= b0 - 2 && x <= b1 + 1) : (x >= b0 - 1 && x <= b1);
+    if (want)
+      tma::bulk_g2s(raw + ((size_t)c * G::RAW_ROWS + (x - top) % G::RAW_ROWS) * G::H,
+                    in + c * G::PLANE + (size_t)((x + G::L) & (G::L - 1)) * G::H, (uint32_t)G::H, br);
+  }
+}
+
+template <int NT, int MINB, int LEAD, int LW>
+__global__ void __launch_bounds__(NT, MINB)
+    sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const __grid_constant__ Params P,
+                 uint32_t tt, int* __restrict__ status) {
+  using G = Geo<NT, LW, LEAD>;
+  constexpr int L = G::L, H = G::H, WPR = G::WPR, R = G::R, RAW_ROWS = G::RAW_ROWS, PK_ROWS = G::PK_ROWS;
+  constexpr size_t PLANE = G::PLANE;
+  constexpr int kRawSlots = LEAD + 1;
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  int* qn = reinterpret_cast<int*>(smem + 64);                    // [colour][3] queue lengths
+  uint32_t* Q = reinterpret_cast<uint32_t*>(smem + 128);          // [colour][3][kQueueCap]
+  uint8_t* raw = smem + 128 + 6 * kQueueCap * 4;                  // [colour][RAW_ROWS][H] bytes
+  uint32_t* pk = reinterpret_cast<uint32_t*>(raw + 2 * (size_t)RAW_ROWS * H);  // [colour][PK_ROWS][WPR]
+  uint32_t* pk1 = pk + PK_ROWS * WPR;
+
+  const int tid = threadIdx.x, rr = tid / WPR, w = tid % WPR;
+  const int b0 = (int)(((long long)blockIdx.x * L) / gridDim.x);
+  const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
+  const int top = b0 - 2;
+  const int J = (b1 - b0 + 4 + R - 1) / R;
+
+  if (tid < kRawSlots) tma::mbar_init(&bar[tid], 1);
+  if (tid < 6) qn[tid] = 0;
+  if (tid == 0) tma::fence_mbar_init();
+  __syncthreads();
+  if (tid < 32)
+    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, in, raw, bar, tid);
+
+  bool ok = true;
+  for (int p = 0; p <= J + 5; ++p) {
+    // queue lengths of buffers no phase touches now (read last phase, next appended after this one)
+    if (tid == 0) {
+      if (p >= 4) qn[(p - 4) % 3] = 0;
+      if (p >= 7) qn[3 + (p - 7) % 3] = 0;
+    }
+    // ---- open sites: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6 (warps 1, 3, ..)
+    {
+      const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
+      if (g >= 0 && g < J) {
+        const int qi = c * 3 + g % 3;
+        const int n = min(qn[qi], kQueueCap);
+        for (int e = (wi >> 1) * 32 + (tid & 31); e < n; e += NT / 2) {
+          const uint32_t dsc = Q[qi * kQueueCap + e];
+          const int k = (int)(dsc & 0x3FFFu), off = (int)(dsc >> 16);
+          const uint32_t m = (dsc >> 14) & 1u, tb = (dsc >> 15) & 1u;
+          const int gr = (top + off + L) & (L - 1);
+          if (open_flips(P, (uint32_t)c, gr, k, m, tt)) {
+            if (c == 0)
+              atomicXor(&pk[(off & (PK_ROWS - 1)) * WPR + (k >> 5)], 1u << plane_pos(k & 31));
+            else
+              out[PLANE + (size_t)gr * H + k] = (uint8_t)(tb ^ 1u);
+          }
+        }
+      }
+    }
+    // ---- bulk copies of group p + LEAD (its slot was packed last phase)
+    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, in, raw, bar, tid);
+    // ---- pack group p
+    if (p < J) {
+      if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
+      const int off = p * R + rr, x = top + off;
+      const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
+      if (ok && x >= b0 - 1 && x <= b1) {
+        const uint4* s = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
+        pk[pi * WPR + w] = pack_bytes(s[0], s[1]);
+      }
+      if (ok && x <= b1 + 1) {
+        const uint4* s = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
+        pk1[pi * WPR + w] = pack_bytes(s[0], s[1]);
+      }
+    }
+    // ---- colour 0 of group p-2
+    if (ok && p >= 2 && p - 2 < J) {
+      const int off = (p - 2) * R + rr, x = top + off;
+      if (x >= b0 - 1 && x <= b1) {
+        const int gr = (x + L) & (L - 1), q = gr & 1, pi = off & (PK_ROWS - 1);
+        const uint32_t t = pk[pi * WPR + w];
+        const uint32_t u = pk1[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
+        const uint32_t d = pk1[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
+        const uint32_t* mr = pk1 + pi * WPR;
+        const uint32_t mid = mr[w];
+        const uint32_t side = q ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
+        const uint4 A = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w), tt);
+        const uint4 B = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
+        uint32_t open, zero;
+        uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
+        if (open) nt ^= enqueue(open, zero, t, qn, Q, 0, (p - 2) % 3, off, w, gr, P, tt);
+        pk[pi * WPR + w] = nt;
+      }
+    }
+    // ---- colour 1 of group p-5, then both colours of its rows to the output
+    if (ok && p >= 5 && p - 5 < J) {
+      const int off = (p - 5) * R + rr, x = top + off;
+      if (x >= b0 && x <= b1 - 1) {
+        const int gr = (x + L) & (L - 1), q = (gr + 1) & 1, pi = off & (PK_ROWS - 1);
+        const uint32_t t = pk1[pi * WPR + w];
+        const uint32_t u = pk[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
+        const uint32_t d = pk[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
+        const uint32_t* mr = pk + pi * WPR;
+        const uint32_t mid = mr[w];
+        const uint32_t side = q ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
+        const uint4 A = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w), tt);
+        const uint4 B = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
+        uint32_t open, zero;
+        uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
+        if (open) nt ^= enqueue(open, zero, t, qn, Q, 1, 3 + (p - 5) % 3, off, w, gr, P, tt);
+        uint4 a, b;
+        unpack_bytes(mid, a, b);
+        uint4* o0 = reinterpret_cast<uint4*>(out + (size_t)gr * H + 32 * w);
+        o0[0] = a;
+        o0[1] = b;
+        unpack_bytes(nt, a, b);
+        uint4* o1 = reinterpret_cast<uint4*>(out + PLANE + (size_t)gr * H + 32 * w);
+        o1[0] = a;
+        o1[1] = b;
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      // a copy did not land: wait (bounded) for the copies still in flight, then report
+      if (tid == 0) {
+        for (int g = p; g < J && g <= p + LEAD; ++g)
+          tma::mbar_wait_bounded(&bar[g % kRawSlots], (uint32_t)((g / kRawSlots) & 1));
+        atomicOr(status, 1);
+      }
+      __syncthreads();
+      return;
+    }
+  }
+}
+
+}  // namespace bits
+}  // namespace mcrg

@@ -1,17 +1,10 @@
 // mcrg_tiled.cu -- HBM-resident lattices (MCRG_SMEM_MAX_L < L <= MCRG_MAX_L).
 //
-// Sweep: one fused two-colour pass per HBM round trip.  A persistent CTA
-// takes tiles of TR rows x TC bytes (per colour).  For each tile it stages,
-// with TMA bulk copies (cp.async.bulk + mbarrier), the old colour-1 rows
-// r0-2 .. r0+TR+1 and colour-0 rows r0-1 .. r0+TR, each widened by 16 bytes
-// on both sides (periodic wrap split into separate copies).  It updates
-// colour 0 on the tile plus its halo, then colour 1 on the tile from the new
-// colour 0, and writes the tile to the other buffer of a ping-pong pair.
-// Halo sites are updated by both neighbouring tiles; the counter-based draws
-// are keyed by the global site, so both compute the same value.  Reads come
-// from one buffer and writes go to the other, so tiles never see each
-// other's output within a sweep.  HBM traffic: one read and one write of
-// every site per sweep (halo re-reads hit L2).
+// Sweep: one fused two-colour pass per HBM round trip (bits::sweep_kernel,
+// mcrg_sweep_bits.cuh): CTAs stream bands of full-width rows through shared
+// memory with bulk copies, update them as bit-plane words and write both
+// colours to the other buffer of a ping-pong pair.  HBM traffic: one read
+// and one write of every site per sweep, plus four halo rows per band.
 //
 // Measurement: every level with side > MCRG_SMEM_MAX_L runs one grid kernel
 // (coupling sums + blocking, straight from global memory); the remaining
@@ -26,8 +19,7 @@
 #include <utility>
 
 #include "mcrg_ops.cuh"
-#include "mcrg_sweep_stream.cuh"
-#include "mcrg_sweep_tiled.cuh"
+#include "mcrg_sweep_bits.cuh"
 #include "mcrg_tiled.cuh"
 
 namespace mcrg {
@@ -137,99 +129,49 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
 
 int g_num_sms = 0;
 
-// Variants of the fused sweep; the autotuner picks one per (L, device) by
-// timing each eligible variant on the live lattice.  "tiles" variants stage
-// TR x TC tiles with halos (any L); "stream" variants walk bands of
-// full-width rows (L = 16384 / R for R rows per step).
+// Variants of the fused sweep: one instantiation per lattice side (L = 64 <<
+// lw) and CTA size; the autotuner picks one per (L, device) by timing each
+// eligible variant on the live lattice.
 struct Variant {
-  const char* name;
-  int TR, TC;  // tile shape (TC = 0 marks a stream variant, TR = its R)
+  int threads, lw, lead;  // threads per CTA, L = 64 << lw, row groups in flight ahead of packing
   const void* kern;
   size_t smem;
 };
 
-#define TILE_VARIANT(TR_, TC_) \
-  Variant { "tiles", TR_, TC_, (const void*)tiled::sweep_kernel<TR_, TC_, 256>, tiled::sweep_smem_bytes<TR_, TC_>() }
-// stream variants are tagged TC = -1 (TR = R rows per step)
-#define STREAM_VARIANT(R_) \
-  Variant { "stream", R_, -1, (const void*)stream::sweep_kernel<R_>, stream::smem_bytes<R_>() }
-
-// two-CTA streaming variants: TC = -(2 + index), TR = 1 (one row per step)
-#define STREAM2_VARIANT(CPR_, NT_, SL_, TAG_)                                                            \
-  Variant { "stream2", 1, -(2 + TAG_), (const void*)stream2::sweep_kernel<CPR_, NT_, SL_>,             \
-            stream2::smem_bytes<CPR_, NT_, SL_>() }
-
-const Variant kVariants[] = {TILE_VARIANT(32, 1024), TILE_VARIANT(16, 1024), TILE_VARIANT(32, 512),
-                             TILE_VARIANT(64, 512),  TILE_VARIANT(16, 512),  TILE_VARIANT(32, 256),
-                             TILE_VARIANT(16, 2048), STREAM_VARIANT(1),      STREAM_VARIANT(2),
-                             STREAM_VARIANT(4),      STREAM_VARIANT(8),      STREAM_VARIANT(16),
-                             STREAM_VARIANT(32),     STREAM2_VARIANT(512, 256, 7, 0),
-                             STREAM2_VARIANT(512, 128, 7, 1), STREAM2_VARIANT(256, 256, 7, 2),
-                             STREAM2_VARIANT(256, 128, 7, 3)};
-// L of a two-CTA streaming variant
-int stream2_L(const Variant& v) {
-  switch (-v.TC - 2) {
-    case 0: case 1: return 16384;
-    default: return 8192;
+#define BITS_VARIANT(NT_, MINB_, LEAD_, LW_)                                                            \
+  Variant {                                                                                              \
+    NT_, LW_, LEAD_, (const void*)bits::sweep_kernel<NT_, MINB_, LEAD_, LW_>, bits::smem_bytes<NT_, LEAD_>() \
   }
-}
-int stream2_threads(const Variant& v) { return (-v.TC - 2) & 1 ? 128 : 256; }
+// three CTA shapes per side: 256 threads x 2 per SM, 512 x 1, 128 x 4 (copy lead 3), and
+// 256 x 3 per SM with a copy lead of 2 (smaller ring, more warps resident)
+#define BITS_VARIANTS_L(LW_)                                                                             \
+  BITS_VARIANT(256, 2, 3, LW_), BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_),             \
+      BITS_VARIANT(256, 3, 2, LW_)
+
+const Variant kVariants[] = {BITS_VARIANT(256, 2, 3, 8), BITS_VARIANT(512, 1, 3, 8), BITS_VARIANT(256, 3, 2, 8),
+                             BITS_VARIANTS_L(7),          BITS_VARIANTS_L(6),          BITS_VARIANTS_L(5),
+                             BITS_VARIANTS_L(4),          BITS_VARIANTS_L(3)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-bool variant_fits(const Variant& v, int L) {
-  if (v.TC < -1) return L == stream2_L(v);
-  if (v.TC < 0) return L * v.TR == 16384;
-  return (L / 2) % v.TC == 0 && L % v.TR == 0;
-}
+bool variant_fits(const Variant& v, int L) { return (64 << v.lw) == L; }
 
-int ctas_for(const Variant& v, int work_items, int threads) {
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, threads, v.smem);
-  if (per_sm < 1) per_sm = 1;
-  int c = g_num_sms * per_sm;
-  return c < work_items ? c : work_items;
-}
+// rows per pipeline group
+int variant_rows(const Variant& v) { return v.threads >> v.lw; }
 
 void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
   const Variant& v = kVariants[vi];
-  if (v.TC < -1) {
-    stream::Params P;
-    memset(&P, 0, sizeof P);
-    P.key = t->key;
-    P.rep = t->replica;
-    P.acc = t->acc;
-    // bands of at least 16 rows, up to two CTAs per SM
-    int bands = t->L / 16;
-    if (bands > 2 * g_num_sms) bands = 2 * g_num_sms;
-    void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-    cudaLaunchKernel(v.kern, dim3(bands), dim3(stream2_threads(v)), args, v.smem, s);
-    return;
-  }
-  if (v.TC < 0) {
-    stream::Params P;
-    memset(&P, 0, sizeof P);
-    P.key = t->key;
-    P.rep = t->replica;
-    P.acc = t->acc;
-    // bands of at least 8R rows, at most one CTA per SM
-    int bands = t->L / (8 * v.TR);
-    if (bands > g_num_sms) bands = g_num_sms;
-    if (bands < 1) bands = 1;
-    void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-    cudaLaunchKernel(v.kern, dim3(bands), dim3(stream::kThreads), args, v.smem, s);
-    return;
-  }
-  tiled::Params P;
+  bits::Params P;
   memset(&P, 0, sizeof P);
-  P.L = t->L;
-  P.h = t->L / 2;
-  P.tiles_x = P.h / v.TC;
-  P.n_tiles = (P.L / v.TR) * P.tiles_x;
-  P.key = t->key;
-  P.rep = t->replica;
-  P.acc = t->acc;
+  bits::fill_params(P, t->key, t->replica, t->acc.thr[0], t->acc.thr[1]);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, v.threads, v.smem);
+  if (per_sm < 1) per_sm = 1;
+  // bands of at least four row groups, as many as fit the GPU at once
+  int bands = t->L / (4 * variant_rows(v));
+  if (bands > g_num_sms * per_sm) bands = g_num_sms * per_sm;
+  if (bands < 1) bands = 1;
   void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-  cudaLaunchKernel(v.kern, dim3(ctas_for(v, P.n_tiles, 256)), dim3(256), args, v.smem, s);
+  cudaLaunchKernel(v.kern, dim3(bands), dim3(v.threads), args, v.smem, s);
 }
 
 int first_tail_level(int L) {
@@ -303,16 +245,11 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   static std::map<std::pair<int, int>, int> cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (const char* force = getenv("MCRG_TILE")) {
-    int tr = 0, tc = 0;
-    if (force[0] == 's' && sscanf(force + 1, "%d", &tr) == 1) tc = -1;
-    if (force[0] == 't' && sscanf(force + 1, "%d", &tc) == 1) {  // two-CTA streaming variant t<index>
-      tr = 1;
-      tc = -(2 + tc);
-    }
-    if (force[0] == 's' || force[0] == 't' || sscanf(force, "%dx%d", &tr, &tc) == 2)
+  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>" or "b<threads>l<lead>" forces a variant
+    int nt = 0, lead = 3;
+    if (force[0] == 'b' && sscanf(force + 1, "%dl%d", &nt, &lead) >= 1)
       for (int v = 0; v < kNumVariants; ++v)
-        if (kVariants[v].TR == tr && kVariants[v].TC == tc && variant_fits(kVariants[v], t->L)) return v;
+        if (kVariants[v].threads == nt && kVariants[v].lead == lead && variant_fits(kVariants[v], t->L)) return v;
   }
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -324,7 +261,7 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   cudaEventCreate(&e1);
   int best = -1;
   float best_ms = 1e30f;
-  const int reps = t->L >= 4096 ? 3 : 10;
+  const int reps = 10;
   for (int v = 0; v < kNumVariants; ++v) {
     if (!variant_fits(kVariants[v], t->L)) continue;
     launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u, s);  // warm-up
@@ -347,10 +284,10 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   return best;
 }
 
-int tiled_variant(TiledLattice* t, int* TR, int* TC) {
+int tiled_variant(TiledLattice* t, int* rows, int* threads) {
   if (t->variant < 0) return -1;
-  if (TR) *TR = kVariants[t->variant].TR;
-  if (TC) *TC = kVariants[t->variant].TC;
+  if (rows) *rows = variant_rows(kVariants[t->variant]);
+  if (threads) *threads = kVariants[t->variant].threads;
   return t->variant;
 }
 

@@ -18,7 +18,7 @@ struct TiledLattice {
   int* d_status = nullptr;                // kernel error flags
   mcrg_moments* d_bins = nullptr;
   int64_t bins_cap = 0;
-  int variant = -1;                       // tile shape picked by the autotuner
+  int variant = -1;                       // sweep variant picked by the autotuner
 };
 
 int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica, const Accept& acc,
@@ -31,8 +31,9 @@ int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s);
 int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, int64_t sweeps_between,
                   int64_t bin_size, int64_t* n_bins, cudaStream_t s);
 mcrg_moments* tiled_bins(TiledLattice* t);
-// Tile shape in use (after the first sweep): returns the variant index.
-int tiled_variant(TiledLattice* t, int* TR, int* TC);
+// Sweep schedule in use (after the first sweep): rows per pipeline group
+// and threads per CTA; returns the variant index.
+int tiled_variant(TiledLattice* t, int* rows, int* threads);
 // Device error flags raised by the tiled kernels (0 = none).
 int tiled_status(TiledLattice* t, cudaStream_t s);
 

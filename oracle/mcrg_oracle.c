@@ -110,19 +110,35 @@ void orc_init_spins(int N, uint64_t seed, uint32_t replica, int8_t* s) {
 
 /* ------------------------------------------------------------------ */
 /* Checkerboard Metropolis sweep (black (i+j even) then white).         */
-/* Site random u32 = r8 << 24 | r24 where                               */
-/*   r8  = byte (k&15) of the P_SWEEP_HI block (row i, group k>>4,      */
-/*         sub = colour c, time = sweep t); byte b of a block is byte   */
-/*         (b&3) of word (b>>2), little-endian;                         */
+/* Site (i, j) of colour c = (i+j)&1 is byte k = j>>1 of its colour     */
+/* row.  Site random u32 = r8 << 24 | r24 where r8 depends on N:        */
+/*   N <= ORC_SMEM_MAX_L (byte draws):                                  */
+/*     r8 = byte (k&15) of the P_SWEEP_HI block (row i, group k>>4,     */
+/*          sub = colour c, time = sweep t); byte b of a block is byte  */
+/*          (b&3) of word (b>>2), little-endian;                        */
+/*   N >  ORC_SMEM_MAX_L (bit-plane draws, 32 sites per plane word):    */
+/*     with w = k>>5, p = k&31 and pos = 8*(p&3) + (p>>2), the planes   */
+/*     W0..W7 are the words of the P_SWEEP_HI blocks (row i, group 2w   */
+/*     and 2w+1, sub = c, time = t) in order, and bit 7-q of r8 is bit  */
+/*     pos of Wq (W0 carries the most significant bit);                 */
 /*   r24 = low 24 bits of word (k&3) of the P_SWEEP_LO block            */
-/*         (row i, group k>>2, sub = c, time = t).                      */
+/*         (row i, group k>>2, sub = c, time = t), both layouts.        */
 /* Flip iff always[m] or u32 < thr[m].                                  */
 /* ------------------------------------------------------------------ */
+#define ORC_SMEM_MAX_L 256
+
+static uint32_t plane_r8(const uint32_t planes[8], int k) {
+    int p = k & 31, pos = 8 * (p & 3) + (p >> 2);
+    uint32_t r8 = 0;
+    for (int q = 0; q < 8; ++q) r8 |= ((planes[q] >> pos) & 1u) << (7 - q);
+    return r8;
+}
 void orc_sweep(int N, int8_t* s, double K, uint64_t seed, uint32_t replica,
                uint32_t t0, int64_t n_sweeps) {
     uint32_t thr[5]; uint8_t always[5];
     orc_thresholds(K, thr, always);
-    uint32_t hi[4], lo[4];
+    uint32_t hi[4], lo[4], planes[8];
+    const int bit_planes = N > ORC_SMEM_MAX_L;
     for (int64_t n = 0; n < n_sweeps; ++n) {
         uint32_t t = t0 + (uint32_t)n;
         for (int c = 0; c < 2; ++c)
@@ -130,7 +146,12 @@ void orc_sweep(int N, int8_t* s, double K, uint64_t seed, uint32_t replica,
                 int last_g = -1;
                 for (int j = ((i + c) & 1); j < N; j += 2) {
                     int k = j >> 1;
-                    if ((k >> 4) != last_g) {
+                    if (bit_planes && (k >> 5) != last_g) {
+                        last_g = k >> 5;
+                        stream(seed, replica, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * last_g), t, planes);
+                        stream(seed, replica, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * last_g + 1), t,
+                               planes + 4);
+                    } else if (!bit_planes && (k >> 4) != last_g) {
                         last_g = k >> 4;
                         stream(seed, replica, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)last_g, t, hi);
                     }
@@ -139,7 +160,7 @@ void orc_sweep(int N, int8_t* s, double K, uint64_t seed, uint32_t replica,
                     int m = (s[ip * N + j] != sv) + (s[im * N + j] != sv) +
                             (s[i * N + jp] != sv) + (s[i * N + jm] != sv);
                     if (always[m]) { s[i * N + j] = (int8_t)-sv; continue; }
-                    uint32_t r8 = (hi[(k & 15) >> 2] >> (8 * (k & 3))) & 0xFFu;
+                    uint32_t r8 = bit_planes ? plane_r8(planes, k) : (hi[(k & 15) >> 2] >> (8 * (k & 3))) & 0xFFu;
                     uint32_t t8 = thr[m] >> 24;
                     int flip;
                     if (r8 != t8) {

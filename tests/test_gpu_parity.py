@@ -305,15 +305,12 @@ def test_device_chain_matches_reference_L8(M, golden):
 
 
 # --------------------------------------------------------------------------
-# every sweep variant of the HBM path (tile shapes and band streaming)
+# every sweep variant of the HBM path (bit-sliced band streaming, threads per CTA)
 # --------------------------------------------------------------------------
 def _variants_for(N):
-    tiles = [(32, 1024), (16, 1024), (32, 512), (64, 512), (16, 512), (32, 256), (16, 2048)]
-    out = ["%dx%d" % (tr, tc) for tr, tc in tiles if (N // 2) % tc == 0 and N % tr == 0]
-    if 16384 % N == 0:
-        out.append("s%d" % (16384 // N))
-    if N == 8192:
-        out += ["t2", "t3"]
+    out = ["b256l3", "b512l3", "b256l2"]
+    if N // 64 <= 128:
+        out.append("b128l3")
     return out
 
 
@@ -326,7 +323,8 @@ def test_every_sweep_variant_bit_exact(M, N, monkeypatch):
         lat = M.Lattice(N, KC, seed=77, replica=4)
         lat.sweep(2)
         got = lat.spins_
-        assert lat.tile_shape() is not None
+        rows, threads = lat.tile_shape()
+        assert threads == int(v[1:].split("l")[0]) and rows * (N // 64) == threads
         lat.close()
         np.testing.assert_array_equal(got, ref, err_msg="variant %s" % v)
 
@@ -338,7 +336,7 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
     init = O.init_spins(N, 5, 0)
     ref = O.sweep(init, KC, 5, 0, 0, 1)
     ref_S = O.couplings(ref, 5)
-    for v in ("s1", "t0", "t1", "32x1024"):
+    for v in ("b256l3", "b512l3", "b256l2"):
         monkeypatch.setenv("MCRG_TILE", v)
         lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
         lat.sweep(1)
