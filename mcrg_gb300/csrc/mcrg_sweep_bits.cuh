@@ -30,7 +30,8 @@
 // The lags make every read in a phase depend only on work that finished
 // before the previous barrier, so one barrier per phase suffices and the
 // rare open sites are resolved compactly by a few lanes instead of stalling
-// every warp that holds one.  Colour 0 is updated on rows b0-1 .. b1 and
+// every warp that holds one (a queue entry is one plane word with open sites:
+// its open, m = 0 and old-value masks).  Colour 0 is updated on rows b0-1 .. b1 and
 // colour 1 on b0 .. b1-1; halo rows are also updated by the neighbouring
 // band with the same draws, so both compute the same values.  Input and
 // output are the two buffers of a ping-pong pair.
@@ -86,11 +87,17 @@ __device__ __forceinline__ uint4 draw(const Params& P, uint32_t purpose, uint32_
 // Row groups of byte rows in flight ahead of packing: LEAD; LEAD + 1 are held
 // per colour.
 constexpr int kPackSlots = 8;          // plane-word groups held per colour
-constexpr int kQueueCap = 256;         // open sites per queue (more are resolved by their owner)
+// Open-site queue entries per buffer: one entry per plane word with open
+// sites (about 0.1 per word at the critical coupling); a word that finds its
+// buffer full is resolved by its owner.
+template <int NT>
+constexpr int queue_cap() {
+  return NT / 4;
+}
 
 template <int NT, int LEAD>
 constexpr size_t smem_bytes() {
-  return 128 + 6 * (size_t)kQueueCap * 4 + 2 * (size_t)(LEAD + 1) * NT * 32 + 2 * (size_t)kPackSlots * NT * 4;
+  return 128 + 6 * (size_t)queue_cap<NT>() * 16 + 2 * (size_t)(LEAD + 1) * NT * 32 + 2 * (size_t)kPackSlots * NT * 4;
 }
 
 // plane bit of site p (0..31) of a word, and its inverse
@@ -140,32 +147,33 @@ __device__ __forceinline__ uint32_t decide(uint32_t t, uint32_t u, uint32_t d, u
   return t ^ (ge2 | br);
 }
 
-// Exact decision of one open site of colour c, row gr, byte k.
-__device__ __forceinline__ bool open_flips(const Params& P, uint32_t c, int gr, int k, uint32_t m, uint32_t tt) {
-  const uint4 lo = draw(P, P_SWEEP_LO, c, (uint32_t)gr, (uint32_t)(k >> 2), tt);
-  const uint32_t th = m ? P.thr1 : P.thr0;
-  return (u4get(lo, k & 3) & 0xFFFFFFu) < (th & 0xFFFFFFu);
-}
-
-// Queues the open sites of word w (row x, band offset off) of colour c;
-// returns the bits of those that did not fit and were resolved here.
-__device__ __forceinline__ uint32_t enqueue(uint32_t open, uint32_t zero, uint32_t t, int* qn, uint32_t* Q, int c,
-                                         int qi, int off, int w, int gr, const Params& P, uint32_t tt) {
-  int slot = atomicAdd(&qn[qi], __popc(open));
-  uint32_t* q = Q + qi * kQueueCap;
+// Open sites of one plane word of colour c (row gr, word w) that flip:
+// each is decided from the low 24 bits of its P_SWEEP_LO draw.
+__device__ __forceinline__ uint32_t open_flips(const Params& P, uint32_t c, int gr, int w, uint32_t open,
+                                               uint32_t zero, uint32_t tt) {
   uint32_t flips = 0;
   while (open) {
     const int pos = __ffs(open) - 1;
     open &= open - 1;
     const int k = 32 * w + plane_site(pos);
-    const uint32_t m = ((zero >> pos) & 1u) ^ 1u;
-    if (slot < kQueueCap)
-      q[slot] = (uint32_t)k | (m << 14) | (((t >> pos) & 1u) << 15) | ((uint32_t)off << 16);
-    else if (open_flips(P, (uint32_t)c, gr, k, m, tt))
-      flips |= 1u << pos;
-    ++slot;
+    const uint4 lo = draw(P, P_SWEEP_LO, c, (uint32_t)gr, (uint32_t)(k >> 2), tt);
+    const uint32_t th = ((zero >> pos) & 1u) ? P.thr0 : P.thr1;
+    if ((u4get(lo, k & 3) & 0xFFFFFFu) < (th & 0xFFFFFFu)) flips |= 1u << pos;
   }
   return flips;
+}
+
+// Queues plane word w (band offset off) of colour c, which has open sites;
+// returns their flips when the buffer is full (resolved here), else 0.
+template <int NT>
+__device__ __forceinline__ uint32_t enqueue(uint32_t open, uint32_t zero, uint32_t t, int off, int w, int gr,
+                                            int c, int qi, int* qn, uint4* Q, const Params& P, uint32_t tt) {
+  const int slot = atomicAdd(&qn[qi], 1);
+  if (slot < queue_cap<NT>()) {
+    Q[qi * queue_cap<NT>() + slot] = make_uint4(open, zero & open, t & open, ((uint32_t)off << 8) | (uint32_t)w);
+    return 0u;
+  }
+  return open_flips(P, (uint32_t)c, gr, w, open, zero, tt);
 }
 
 // Geometry of one instantiation: lattice side L = 64 << LW, NT threads.
@@ -202,6 +210,39 @@ __device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, cons
   }
 }
 
+// Resolves the open sites queued for colour c by group g: entries first,
+// first + stride, ... of the buffer; flips go to the packed colour-0 row in
+// shared memory (c = 0) or to the bytes already written to HBM (c = 1).
+template <int NT, int LW, int LEAD>
+__device__ __forceinline__ void resolve_queue(int c, int g, int first, int stride, const int* qn, const uint4* Q,
+                                              uint32_t* pk, uint8_t* out, int top, const Params& P, uint32_t tt) {
+  using G = Geo<NT, LW, LEAD>;
+  constexpr int CAP = queue_cap<NT>();
+  const int qi = c * 3 + g % 3;
+  const int n = min(qn[qi], CAP);
+  for (int e = first; e < n; e += stride) {
+    const uint4 ent = Q[qi * CAP + e];
+    const int off = (int)(ent.w >> 8), ww = (int)(ent.w & 0xFFu);
+    const int gr = (top + off + G::L) & (G::L - 1);
+    const uint32_t fl = open_flips(P, (uint32_t)c, gr, ww, ent.x, ent.y, tt);
+    if (fl == 0u) continue;
+    if (c == 0) {
+      atomicXor(&pk[(off & (G::PK_ROWS - 1)) * G::WPR + ww], fl);
+    } else {
+      uint32_t f = fl;
+      while (f) {
+        const int pos = __ffs(f) - 1;
+        f &= f - 1;
+        out[G::PLANE + (size_t)gr * G::H + 32 * ww + plane_site(pos)] = (uint8_t)(((ent.z >> pos) & 1u) ^ 1u);
+      }
+    }
+  }
+}
+
+// NT compute threads, one plane word per colour per group each; warp 0 also
+// issues the bulk copies.  (A dedicated helper warp for the copies and the
+// open sites, and drawing the Philox blocks ahead of the copy wait, both
+// measured slower on GB300.)
 template <int NT, int MINB, int LEAD, int LW>
 __global__ void __launch_bounds__(NT, MINB)
     sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const __grid_constant__ Params P,
@@ -209,16 +250,17 @@ __global__ void __launch_bounds__(NT, MINB)
   using G = Geo<NT, LW, LEAD>;
   constexpr int L = G::L, H = G::H, WPR = G::WPR, R = G::R, RAW_ROWS = G::RAW_ROWS, PK_ROWS = G::PK_ROWS;
   constexpr size_t PLANE = G::PLANE;
-  constexpr int kRawSlots = LEAD + 1;
+  constexpr int kRawSlots = LEAD + 1, CAP = queue_cap<NT>();
   extern __shared__ __align__(128) uint8_t smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   int* qn = reinterpret_cast<int*>(smem + 64);                    // [colour][3] queue lengths
-  uint32_t* Q = reinterpret_cast<uint32_t*>(smem + 128);          // [colour][3][kQueueCap]
-  uint8_t* raw = smem + 128 + 6 * kQueueCap * 4;                  // [colour][RAW_ROWS][H] bytes
+  uint4* Q = reinterpret_cast<uint4*>(smem + 128);                // [colour][3][CAP] entries
+  uint8_t* raw = smem + 128 + 6 * CAP * 16;                       // [colour][RAW_ROWS][H] bytes
   uint32_t* pk = reinterpret_cast<uint32_t*>(raw + 2 * (size_t)RAW_ROWS * H);  // [colour][PK_ROWS][WPR]
   uint32_t* pk1 = pk + PK_ROWS * WPR;
 
-  const int tid = threadIdx.x, rr = tid / WPR, w = tid % WPR;
+  const int tid = threadIdx.x, w = tid % WPR, lane = tid & 31;
+  const int rr = (R == 1) ? 0 : tid / WPR;  // row within a group (uniform when groups are one row)
   const int b0 = (int)(((long long)blockIdx.x * L) / gridDim.x);
   const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
   const int top = b0 - 2;
@@ -229,7 +271,7 @@ __global__ void __launch_bounds__(NT, MINB)
   if (tid == 0) tma::fence_mbar_init();
   __syncthreads();
   if (tid < 32)
-    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, in, raw, bar, tid);
+    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, in, raw, bar, lane);
 
   bool ok = true;
   for (int p = 0; p <= J + 5; ++p) {
@@ -238,77 +280,64 @@ __global__ void __launch_bounds__(NT, MINB)
       if (p >= 4) qn[(p - 4) % 3] = 0;
       if (p >= 7) qn[3 + (p - 7) % 3] = 0;
     }
-    // ---- open sites: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6 (warps 1, 3, ..)
+    // ---- open sites queued last phase: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6
     {
       const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
-      if (g >= 0 && g < J) {
-        const int qi = c * 3 + g % 3;
-        const int n = min(qn[qi], kQueueCap);
-        for (int e = (wi >> 1) * 32 + (tid & 31); e < n; e += NT / 2) {
-          const uint32_t dsc = Q[qi * kQueueCap + e];
-          const int k = (int)(dsc & 0x3FFFu), off = (int)(dsc >> 16);
-          const uint32_t m = (dsc >> 14) & 1u, tb = (dsc >> 15) & 1u;
-          const int gr = (top + off + L) & (L - 1);
-          if (open_flips(P, (uint32_t)c, gr, k, m, tt)) {
-            if (c == 0)
-              atomicXor(&pk[(off & (PK_ROWS - 1)) * WPR + (k >> 5)], 1u << plane_pos(k & 31));
-            else
-              out[PLANE + (size_t)gr * H + k] = (uint8_t)(tb ^ 1u);
-          }
-        }
-      }
+      if (g >= 0 && g < J) resolve_queue<NT, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, P, tt);
     }
     // ---- bulk copies of group p + LEAD (its slot was packed last phase)
-    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, in, raw, bar, tid);
+    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, in, raw, bar, lane);
     // ---- pack group p
     if (p < J) {
       if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
       const int off = p * R + rr, x = top + off;
       const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
       if (ok && x >= b0 - 1 && x <= b1) {
-        const uint4* s = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
-        pk[pi * WPR + w] = pack_bytes(s[0], s[1]);
+        const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
+        pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
       }
       if (ok && x <= b1 + 1) {
-        const uint4* s = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
-        pk1[pi * WPR + w] = pack_bytes(s[0], s[1]);
+        const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
+        pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
       }
     }
     // ---- colour 0 of group p-2
-    if (ok && p >= 2 && p - 2 < J) {
+    {
       const int off = (p - 2) * R + rr, x = top + off;
-      if (x >= b0 - 1 && x <= b1) {
-        const int gr = (x + L) & (L - 1), q = gr & 1, pi = off & (PK_ROWS - 1);
+      if (ok && p >= 2 && p - 2 < J && x >= b0 - 1 && x <= b1) {
+        const int gr = (x + L) & (L - 1), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk[pi * WPR + w];
         const uint32_t u = pk1[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t d = pk1[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t* mr = pk1 + pi * WPR;
         const uint32_t mid = mr[w];
-        const uint32_t side = q ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
+        const uint32_t side =
+            (gr & 1) ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
         const uint4 A = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w), tt);
         const uint4 B = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue(open, zero, t, qn, Q, 0, (p - 2) % 3, off, w, gr, P, tt);
+        if (open) nt ^= enqueue<NT>(open, zero, t, off, w, gr, 0, (p - 2) % 3, qn, Q, P, tt);
         pk[pi * WPR + w] = nt;
       }
     }
     // ---- colour 1 of group p-5, then both colours of its rows to the output
-    if (ok && p >= 5 && p - 5 < J) {
+    {
       const int off = (p - 5) * R + rr, x = top + off;
-      if (x >= b0 && x <= b1 - 1) {
-        const int gr = (x + L) & (L - 1), q = (gr + 1) & 1, pi = off & (PK_ROWS - 1);
+      if (ok && p >= 5 && p - 5 < J && x >= b0 && x <= b1 - 1) {
+        const int gr = (x + L) & (L - 1), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk1[pi * WPR + w];
         const uint32_t u = pk[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t d = pk[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t* mr = pk + pi * WPR;
         const uint32_t mid = mr[w];
-        const uint32_t side = q ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
+        const uint32_t side =
+            ((gr + 1) & 1) ? right_sites(mid, mr[(w + 1) & (WPR - 1)]) : left_sites(mid, mr[(w - 1) & (WPR - 1)]);
         const uint4 A = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w), tt);
         const uint4 B = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue(open, zero, t, qn, Q, 1, 3 + (p - 5) % 3, off, w, gr, P, tt);
+        if (open) nt ^= enqueue<NT>(open, zero, t, off, w, gr, 1, 3 + (p - 5) % 3, qn, Q, P, tt);
         uint4 a, b;
         unpack_bytes(mid, a, b);
         uint4* o0 = reinterpret_cast<uint4*>(out + (size_t)gr * H + 32 * w);

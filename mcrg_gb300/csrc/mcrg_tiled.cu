@@ -142,16 +142,17 @@ struct Variant {
   Variant {                                                                                              \
     NT_, LW_, LEAD_, (const void*)bits::sweep_kernel<NT_, MINB_, LEAD_, LW_>, bits::smem_bytes<NT_, LEAD_>() \
   }
-// three CTA shapes per side: 256 threads x 2 per SM, 512 x 1, 128 x 4 (copy lead 3), and
-// 256 x 3 per SM with a copy lead of 2 (smaller ring, more warps resident)
+// per side: 256 threads x 3 CTAs per SM (copy lead 2), x 4 (lead 1), x 2 (lead 3), 512 x 1, 128 x 4
 #define BITS_VARIANTS_L(LW_)                                                                             \
-  BITS_VARIANT(256, 2, 3, LW_), BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_),             \
-      BITS_VARIANT(256, 3, 2, LW_)
+  BITS_VARIANT(256, 3, 2, LW_), BITS_VARIANT(256, 4, 1, LW_), BITS_VARIANT(256, 2, 3, LW_),             \
+      BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_)
 
-const Variant kVariants[] = {BITS_VARIANT(256, 2, 3, 8), BITS_VARIANT(512, 1, 3, 8), BITS_VARIANT(256, 3, 2, 8),
-                             BITS_VARIANTS_L(7),          BITS_VARIANTS_L(6),          BITS_VARIANTS_L(5),
-                             BITS_VARIANTS_L(4),          BITS_VARIANTS_L(3)};
+const Variant kVariants[] = {BITS_VARIANT(256, 3, 2, 8), BITS_VARIANT(256, 4, 1, 8), BITS_VARIANT(256, 2, 3, 8),
+                             BITS_VARIANT(512, 1, 3, 8), BITS_VARIANTS_L(7),          BITS_VARIANTS_L(6),
+                             BITS_VARIANTS_L(5),          BITS_VARIANTS_L(4),          BITS_VARIANTS_L(3)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+int block_threads(const Variant& v) { return v.threads; }
 
 bool variant_fits(const Variant& v, int L) { return (64 << v.lw) == L; }
 
@@ -164,14 +165,14 @@ void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* o
   memset(&P, 0, sizeof P);
   bits::fill_params(P, t->key, t->replica, t->acc.thr[0], t->acc.thr[1]);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, v.threads, v.smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, block_threads(v), v.smem);
   if (per_sm < 1) per_sm = 1;
   // bands of at least four row groups, as many as fit the GPU at once
   int bands = t->L / (4 * variant_rows(v));
   if (bands > g_num_sms * per_sm) bands = g_num_sms * per_sm;
   if (bands < 1) bands = 1;
   void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-  cudaLaunchKernel(v.kern, dim3(bands), dim3(v.threads), args, v.smem, s);
+  cudaLaunchKernel(v.kern, dim3(bands), dim3(block_threads(v)), args, v.smem, s);
 }
 
 int first_tail_level(int L) {
@@ -245,8 +246,8 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   static std::map<std::pair<int, int>, int> cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>" or "b<threads>l<lead>" forces a variant
-    int nt = 0, lead = 3;
+  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>l<lead>" forces a variant
+    int nt = 0, lead = 2;
     if (force[0] == 'b' && sscanf(force + 1, "%dl%d", &nt, &lead) >= 1)
       for (int v = 0; v < kNumVariants; ++v)
         if (kVariants[v].threads == nt && kVariants[v].lead == lead && variant_fits(kVariants[v], t->L)) return v;

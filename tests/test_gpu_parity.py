@@ -308,7 +308,7 @@ def test_device_chain_matches_reference_L8(M, golden):
 # every sweep variant of the HBM path (bit-sliced band streaming, threads per CTA)
 # --------------------------------------------------------------------------
 def _variants_for(N):
-    out = ["b256l3", "b512l3", "b256l2"]
+    out = ["b256l2", "b256l1", "b256l3", "b512l3"]
     if N // 64 <= 128:
         out.append("b128l3")
     return out
@@ -336,7 +336,7 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
     init = O.init_spins(N, 5, 0)
     ref = O.sweep(init, KC, 5, 0, 0, 1)
     ref_S = O.couplings(ref, 5)
-    for v in ("b256l3", "b512l3", "b256l2"):
+    for v in ("b256l2", "b256l1", "b512l3"):
         monkeypatch.setenv("MCRG_TILE", v)
         lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
         lat.sweep(1)
