@@ -108,6 +108,20 @@ typedef struct {
   mcrg_i128 SbSb[MCRG_MAX_LEVELS * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS];
 } mcrg_moments;
 
+/* Renormalisation-flow moments of one chain (coupling 0, nearest
+ * neighbours): S[l] = sum over samples of S_nn at level l, S0S[l] = sum of
+ * S_nn(level l) * S_nn(level 0), for l = 0 .. n_levels.  They are the sums of
+ * the sample loop of approx_critical_point (src/mcrg.cpp:225-258): for the
+ * lattice of side L, SL = S[0], SLb(n) = S[n+1], SLb*SL = S0S[n+1]; for the
+ * lattice of side L/b, SS = S[0], SSb(n) = S[n], SSb*SS = S0S[n]. */
+typedef struct {
+  int32_t n_levels;
+  int32_t pad;
+  int64_t n_samples;
+  int64_t S[MCRG_MAX_LEVELS + 1];
+  mcrg_i128 S0S[MCRG_MAX_LEVELS + 1];
+} mcrg_flow_moments;
+
 typedef struct mcrg_ctx mcrg_ctx;
 
 const char* mcrg_strerror(int code);
@@ -151,6 +165,14 @@ int mcrg_interactions(mcrg_ctx* ctx, int64_t* out);
  * q < n_bins_cap (binned error bars). */
 int mcrg_measure(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total,
                  int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap);
+
+/* Replaces the sample loop of approx_critical_point (src/mcrg.cpp:225-258)
+ * for one of its two lattices: n_samples x (sweeps_between sweeps, then the
+ * nearest-neighbour sums of every level and their products with level 0),
+ * on the device, exactly in integers.  The host matching step
+ * (src/mcrg.cpp:283-301) combines the moments of a context of side L and one
+ * of side L/b at the same K. */
+int mcrg_measure_flow(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_flow_moments* out);
 
 /* Sweep and sample counters (the Philox time words of the next sweep / sample). */
 int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);

@@ -128,6 +128,17 @@ class Lattice:
         check(lib().mcrg_measure(self._ctx, n_samples, sweeps_between, C.byref(tot), 0, None, 0), "mcrg_measure")
         return moments_from_c(tot), []
 
+    def measure_flow(self, n_samples: int, sweeps_between: int = 1):
+        """Flow moments (src/mcrg.cpp:225-258 for one lattice): sums of S_nn per level
+        and of S_nn(level) * S_nn(level 0), exact integers."""
+        from .critical import FlowMoments
+
+        m = _abi.FlowMoments()
+        check(lib().mcrg_measure_flow(self._ctx, n_samples, sweeps_between, C.byref(m)), "mcrg_measure_flow")
+        nl = m.n_levels
+        return FlowMoments(int(m.n_samples), [int(m.S[l]) for l in range(nl + 1)],
+                           [_i128(m.S0S[l]) for l in range(nl + 1)])
+
     def counters(self) -> tuple[int, int]:
         t = C.c_uint64()
         n = C.c_uint64()
@@ -182,6 +193,17 @@ class MonteCarloRenormalizationGroup:
         self.device = device
         self.sweeps_between = sweeps_between
         self.last = None
+
+    def locate_critical_point(self, n_iterations: int, n_samples_eq: int, n_samples: int, L: int, K0: float,
+                              write_file: bool = False) -> float:
+        """src/mcrg.cpp:145-189 (see mcrg_gb300.critical)."""
+        from .critical import locate_critical_point
+
+        K, rows = locate_critical_point(n_iterations, n_samples_eq, n_samples, L, K0, seed=self.seed,
+                                        device=self.device, write_file=write_file,
+                                        sweeps_between=self.sweeps_between)
+        self.last_flow = rows
+        return K
 
     def calc_critical_exponent(self, n_samples_eq: int, n_samples: int, N: int, K: float,
                                bin_size: int = 0, write_file: bool = False) -> list[tuple[int, float, float]]:

@@ -47,6 +47,11 @@ class Moments(C.Structure):
                 ("S", C.c_int64 * NS), ("SbS", I128 * NP), ("SbSb", I128 * NP)]
 
 
+class FlowMoments(C.Structure):
+    _fields_ = [("n_levels", C.c_int32), ("pad", C.c_int32), ("n_samples", C.c_int64),
+                ("S", C.c_int64 * (MAX_LEVELS + 1)), ("S0S", I128 * (MAX_LEVELS + 1))]
+
+
 class Request(C.Structure):
     _fields_ = [("L", C.c_int32), ("n_levels", C.c_int32), ("n_couplings", C.c_int32), ("flags", C.c_int32),
                 ("K", C.c_double), ("seed", C.c_uint64), ("replica", C.c_uint32), ("pad", C.c_uint32),
@@ -76,6 +81,7 @@ _SIGS = {
     "mcrg_block": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "mcrg_interactions": (C.c_int, [C.c_void_p, P(C.c_int64)]),
     "mcrg_measure": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(Moments), C.c_int64, P(Moments), C.c_int64]),
+    "mcrg_measure_flow": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(FlowMoments)]),
     "mcrg_counters": (C.c_int, [C.c_void_p, P(C.c_uint64), P(C.c_uint64)]),
     "mcrg_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
     "mcrg_tile_shape": (C.c_int, [C.c_void_p, P(C.c_int32), P(C.c_int32)]),

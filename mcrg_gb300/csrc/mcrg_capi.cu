@@ -131,7 +131,7 @@ int ensure_bins(mcrg_ctx* c, int64_t n) {
 
 // Runs one resident chain job for the context and returns the device bins.
 int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_between, int64_t bin_size,
-                 int64_t* n_bins_out) {
+                 int64_t* n_bins_out, bool flow = false) {
   ChainJob j;
   memset(&j, 0, sizeof j);
   j.L = c->cfg.L;
@@ -150,6 +150,7 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   j.bin_size = bin_size;
   j.state = c->d_state;
   j.acc = c->acc;
+  j.flow = flow ? 1 : 0;
   int64_t nb = n_samples > 0 ? (n_samples + bin_size - 1) / bin_size : 0;
   if (nb > 0) {
     int rc = ensure_bins(c, nb);
@@ -324,8 +325,10 @@ int mcrg_sweep(mcrg_ctx* c, int64_t n_sweeps) {
   return run_resident(c, n_sweeps, 0, 0, 1, &nb);
 }
 
-int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total, int64_t bin_size,
-                 mcrg_moments* bins, int64_t n_bins_cap) {
+// Sample loop shared by mcrg_measure (T-matrix moments) and
+// mcrg_measure_flow (flow moments, flow = true).
+static int measure_impl(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total,
+                        int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap, bool flow) {
   if (!c || n_samples < 0 || sweeps_between < 0) return MCRG_EINVAL;
   if (bins && (bin_size <= 0 || bin_size > kMaxDeviceBin || n_bins_cap < 0)) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
@@ -347,7 +350,7 @@ int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_mo
   int64_t nb = 0;
   if (c->is_tiled) {
     int rc = tiled_measure(&c->tiled, (uint32_t)c->t, (uint32_t)c->n, n_samples, sweeps_between, dev_bin, &nb,
-                           c->stream);
+                           c->stream, flow);
     if (rc) return rc;
     c->t += (uint64_t)(n_samples * sweeps_between);
     c->n += (uint64_t)n_samples;
@@ -355,7 +358,7 @@ int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_mo
     CK(cudaMemcpyAsync(h.data(), tiled_bins(&c->tiled), sizeof(mcrg_moments) * (size_t)nb,
                        cudaMemcpyDeviceToHost, c->stream));
   } else {
-    int rc = run_resident(c, 0, n_samples, sweeps_between, dev_bin, &nb);
+    int rc = run_resident(c, 0, n_samples, sweeps_between, dev_bin, &nb, flow);
     if (rc) return rc;
     h.resize((size_t)nb);
     CK(cudaMemcpyAsync(h.data(), c->d_bins, sizeof(mcrg_moments) * (size_t)nb, cudaMemcpyDeviceToHost,
@@ -365,6 +368,26 @@ int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_mo
   for (int64_t q = 0; q < nb; ++q) {
     if (total) add_moments(total, &h[(size_t)q]);
     if (bins && q < n_bins_cap) bins[q] = h[(size_t)q];
+  }
+  return MCRG_OK;
+}
+
+int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total, int64_t bin_size,
+                 mcrg_moments* bins, int64_t n_bins_cap) {
+  return measure_impl(c, n_samples, sweeps_between, total, bin_size, bins, n_bins_cap, false);
+}
+
+int mcrg_measure_flow(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_flow_moments* out) {
+  if (!c || !out) return MCRG_EINVAL;
+  mcrg_moments m;
+  const int rc = measure_impl(c, n_samples, sweeps_between, &m, 0, nullptr, 0, true);
+  if (rc) return rc;
+  memset(out, 0, sizeof *out);
+  out->n_levels = c->n_levels;
+  out->n_samples = m.n_samples;
+  for (int l = 0; l <= c->n_levels; ++l) {
+    out->S[l] = m.S[l * MCRG_MAX_COUPLINGS];
+    out->S0S[l] = m.SbSb[l * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS];
   }
   return MCRG_OK;
 }

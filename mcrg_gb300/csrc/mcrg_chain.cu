@@ -50,7 +50,8 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   int* S = reinterpret_cast<int*>(smem + plan.s_off);
   int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
   long long* macc = reinterpret_cast<long long*>(smem + plan.acc_off);
-  const int E = plan.E;
+  // moment entries: T-matrix moments (S, Sb S, Sb Sb) or flow moments (S_l, S_l S_0 of coupling 0)
+  const int E = J.flow ? 2 * (nl + 1) : plan.E;
   uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (threadIdx.x >> 5) * kOpenPerWarp;
   const bool vec = acc.fast && L >= 16;
 
@@ -66,7 +67,13 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   //      and the output slot (kind << 16 | index into S / SbS / SbSb)
   for (int e = tid; e < E; e += T) {
     int x, y, out;
-    if (e < (nl + 1) * C) {
+    if (J.flow) {
+      // e <= nl: sum of S_e (coupling 0) into S[e*5]; else S_l S_0 into SbSb[l*25], l = e - nl - 1
+      const int l = e <= nl ? e : e - nl - 1;
+      x = l * MCRG_MAX_COUPLINGS;
+      y = e <= nl ? 0xFFFF : 0;
+      out = e <= nl ? x : ((2 << 16) | (l * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS));
+    } else if (e < (nl + 1) * C) {
       const int l = e / C, c = e % C;
       x = l * MCRG_MAX_COUPLINGS + c;
       y = 0xFFFF;

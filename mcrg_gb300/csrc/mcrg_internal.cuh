@@ -22,6 +22,8 @@ struct ChainJob {
   uint8_t* state;     // L*L bytes: colour-0 array then colour-1 array
   mcrg_moments* bins; // ceil(n_samples / bin_size) outputs, zeroed by the host
   Accept acc;
+  int32_t flow;       // 1: flow moments (sum S_l and S_l * S_0 of coupling 0) instead of the T-matrix moments
+  int32_t pad;
 };
 
 // Shared-memory plan of a resident lattice, its blocked levels and (when
@@ -32,7 +34,8 @@ struct SmemPlan {
   int tab_off;  // int2 per moment entry: (x | y << 16, output index)
   int acc_off;  // int64 per moment entry
   int scr_off;  // uint32 open-site scratch: 64 per warp, up to 8 warps
-  int E;        // moment entries
+  int E;        // moment entries of the T-matrix moments
+  int Ecap;     // entries the table holds (also fits the 2 (n_levels + 1) flow moments)
   int bytes;
 };
 
@@ -46,10 +49,11 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
   p.s_off = off;
   off += ((MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS * 4 + 15) / 16 * 16;
   p.E = C > 0 ? (n_levels + 1) * C + 2 * n_levels * C * C : 0;
+  p.Ecap = C > 0 ? (p.E > 2 * (n_levels + 1) ? p.E : 2 * (n_levels + 1)) : 0;
   p.tab_off = off;
-  off += ((p.E * 8 + 15) / 16) * 16;
+  off += ((p.Ecap * 8 + 15) / 16) * 16;
   p.acc_off = off;
-  off += p.E * 8;
+  off += p.Ecap * 8;
   p.scr_off = off;
   off += 8 * 64 * 4;
   p.bytes = (off + 15) / 16 * 16;

@@ -62,6 +62,7 @@ struct TailJob {
   mcrg_moments* bin;
   Key key;
   uint32_t rep, sample;
+  int flow;                  // 1: flow moments (sum S_l and S_l * S_0 of coupling 0)
 };
 
 __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
@@ -100,10 +101,22 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
       if (x >= lt * MCRG_MAX_COUPLINGS) Sv[x] = St[x];
   }
   __syncthreads();
-  const int E = (nl + 1) * C + 2 * nl * C * C;
+  const int E = J.flow ? 2 * (nl + 1) : (nl + 1) * C + 2 * nl * C * C;
   mcrg_moments* out = J.bin;
   for (int e = tid; e < E; e += T) {
-    if (e < (nl + 1) * C) {
+    if (J.flow) {
+      // e <= nl: sum of S_e (coupling 0); else S_l S_0 into SbSb[l*25], l = e - nl - 1
+      const int l = e <= nl ? e : e - nl - 1;
+      if (e <= nl) {
+        out->S[l * MCRG_MAX_COUPLINGS] += Sv[l * MCRG_MAX_COUPLINGS];
+      } else {
+        mcrg_i128* dstv = out->SbSb + l * MCRG_MAX_COUPLINGS * MCRG_MAX_COUPLINGS;
+        __int128 cur = ((__int128)dstv->hi << 64) | (__int128)dstv->lo;
+        cur += (__int128)Sv[l * MCRG_MAX_COUPLINGS] * (__int128)Sv[0];
+        dstv->lo = (uint64_t)cur;
+        dstv->hi = (int64_t)(cur >> 64);
+      }
+    } else if (e < (nl + 1) * C) {
       const int l = e / C, c = e % C;
       out->S[l * MCRG_MAX_COUPLINGS + c] += Sv[l * MCRG_MAX_COUPLINGS + c];
     } else {
@@ -136,18 +149,20 @@ struct Variant {
   int threads, lw, lead;  // threads per CTA, L = 64 << lw, row groups in flight ahead of packing
   const void* kern;
   size_t smem;
+  int waves;              // bands = waves x resident CTAs (two waves measured slower: more halo rows)
 };
 
-#define BITS_VARIANT(NT_, MINB_, LEAD_, LW_)                                                            \
+#define BITS_VARIANT_W(NT_, MINB_, LEAD_, LW_, W_)                                                      \
   Variant {                                                                                              \
-    NT_, LW_, LEAD_, (const void*)bits::sweep_kernel<NT_, MINB_, LEAD_, LW_>, bits::smem_bytes<NT_, LEAD_>() \
+    NT_, LW_, LEAD_, (const void*)bits::sweep_kernel<NT_, MINB_, LEAD_, LW_>, bits::smem_bytes<NT_, LEAD_>(), W_ \
   }
+#define BITS_VARIANT(NT_, MINB_, LEAD_, LW_) BITS_VARIANT_W(NT_, MINB_, LEAD_, LW_, 1)
 // per side: 256 threads x 3 CTAs per SM (copy lead 2), x 4 (lead 1), x 2 (lead 3), 512 x 1, 128 x 4
 #define BITS_VARIANTS_L(LW_)                                                                             \
   BITS_VARIANT(256, 3, 2, LW_), BITS_VARIANT(256, 4, 1, LW_), BITS_VARIANT(256, 2, 3, LW_),             \
       BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_)
 
-const Variant kVariants[] = {BITS_VARIANT(256, 3, 2, 8), BITS_VARIANT(256, 4, 1, 8), BITS_VARIANT(256, 2, 3, 8),
+const Variant kVariants[] = {BITS_VARIANT(256, 4, 1, 8), BITS_VARIANT(256, 3, 2, 8), BITS_VARIANT(256, 2, 3, 8),
                              BITS_VARIANT(512, 1, 3, 8), BITS_VARIANTS_L(7),          BITS_VARIANTS_L(6),
                              BITS_VARIANTS_L(5),          BITS_VARIANTS_L(4),          BITS_VARIANTS_L(3)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
@@ -167,9 +182,9 @@ void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* o
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, block_threads(v), v.smem);
   if (per_sm < 1) per_sm = 1;
-  // bands of at least four row groups, as many as fit the GPU at once
+  // bands of at least four row groups, `waves` times as many as fit the GPU at once
   int bands = t->L / (4 * variant_rows(v));
-  if (bands > g_num_sms * per_sm) bands = g_num_sms * per_sm;
+  if (bands > v.waves * g_num_sms * per_sm) bands = v.waves * g_num_sms * per_sm;
   if (bands < 1) bands = 1;
   void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
   cudaLaunchKernel(v.kern, dim3(bands), dim3(block_threads(v)), args, v.smem, s);
@@ -246,11 +261,13 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   static std::map<std::pair<int, int>, int> cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>l<lead>" forces a variant
-    int nt = 0, lead = 2;
-    if (force[0] == 'b' && sscanf(force + 1, "%dl%d", &nt, &lead) >= 1)
+  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>l<lead>[w<waves>]" forces a variant
+    int nt = 0, lead = 2, waves = 1;
+    if (force[0] == 'b' && sscanf(force + 1, "%dl%dw%d", &nt, &lead, &waves) >= 1)
       for (int v = 0; v < kNumVariants; ++v)
-        if (kVariants[v].threads == nt && kVariants[v].lead == lead && variant_fits(kVariants[v], t->L)) return v;
+        if (kVariants[v].threads == nt && kVariants[v].lead == lead && kVariants[v].waves == waves &&
+            variant_fits(kVariants[v], t->L))
+          return v;
   }
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -305,7 +322,7 @@ int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
 }
 
-static int measure_one(TiledLattice* t, uint32_t sample, mcrg_moments* bin, cudaStream_t s) {
+static int measure_one(TiledLattice* t, uint32_t sample, mcrg_moments* bin, bool flow, cudaStream_t s) {
   const int L = t->L, nl = t->nl, lt = t->n_hbm;
   const uint8_t* cur = t->buf[t->cur];
   for (int l = 0; l < lt && l <= nl; ++l) {
@@ -331,13 +348,14 @@ static int measure_one(TiledLattice* t, uint32_t sample, mcrg_moments* bin, cuda
   J.key = t->key;
   J.rep = t->replica;
   J.sample = sample;
+  J.flow = flow ? 1 : 0;
   const size_t sm = (lt <= nl) ? (size_t)make_plan(L >> lt, nl - lt).bytes : 16;
   tail_kernel<<<1, 256, sm, s>>>(J);
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
 }
 
 int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, int64_t sweeps_between,
-                  int64_t bin_size, int64_t* n_bins, cudaStream_t s) {
+                  int64_t bin_size, int64_t* n_bins, cudaStream_t s, bool flow) {
   const int64_t nb = (n_samples + bin_size - 1) / bin_size;
   if (nb > t->bins_cap) {
     cudaFree(t->d_bins);
@@ -352,7 +370,7 @@ int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, 
     int rc = tiled_sweeps(t, tt, sweeps_between, s);
     if (rc) return rc;
     tt += (uint32_t)sweeps_between;
-    rc = measure_one(t, n0 + (uint32_t)k, t->d_bins + k / bin_size, s);
+    rc = measure_one(t, n0 + (uint32_t)k, t->d_bins + k / bin_size, flow, s);
     if (rc) return rc;
   }
   *n_bins = nb;

@@ -28,8 +28,10 @@ uint8_t* tiled_state(TiledLattice* t);
 // n sweeps starting at sweep index t0 (one fused two-colour pass per sweep).
 int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s);
 // n_samples x (sweeps_between sweeps + measurement); bins of bin_size samples.
+// flow: accumulate the flow moments (sum S_l in S[l*5], sum S_l S_0 in
+// SbSb[l*25], coupling 0) instead of the T-matrix moments.
 int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, int64_t sweeps_between,
-                  int64_t bin_size, int64_t* n_bins, cudaStream_t s);
+                  int64_t bin_size, int64_t* n_bins, cudaStream_t s, bool flow = false);
 mcrg_moments* tiled_bins(TiledLattice* t);
 // Sweep schedule in use (after the first sweep): rows per pipeline group
 // and threads per CTA; returns the variant index.

@@ -154,3 +154,93 @@ void MonteCarloRenormalizationGroup::calc_critical_exponent(int n_samples_eq, in
   printf("\n* Critical exponent: nu = %lf\n", nu);
   if (f) fclose(f);
 }
+
+// ---------------------------------------------------------------------------
+// Critical point by flow matching (src/mcrg.cpp:145-301).  The sample loop of
+// both lattices runs on the device (mcrg_measure_flow); the connected parts
+// <x y> - <x><y> are formed from the exact integer sums before dividing.
+// ---------------------------------------------------------------------------
+namespace {
+
+// (n sum_xy - sum_x sum_y) / n^2
+long double connected(const mcrg_i128& sum_xy, int64_t sum_x, int64_t sum_y, int64_t n) {
+  const __int128 xy = ((__int128)sum_xy.hi << 64) | (__int128)sum_xy.lo;
+  const __int128 num = xy * (__int128)n - (__int128)sum_x * (__int128)sum_y;
+  return (long double)num / ((long double)n * (long double)n);
+}
+
+void flow_of(int side, double K, uint64_t seed, uint32_t replica, int device, int n_eq, int n_samples,
+             mcrg_flow_moments* out) {
+  mcrg_cfg cfg{};
+  cfg.L = side;
+  cfg.b = 2;
+  cfg.n_levels = -1;
+  cfg.n_couplings = 1;
+  cfg.K = K;
+  cfg.seed = seed;
+  cfg.replica = replica;
+  cfg.device = device;
+  mcrg_ctx* ctx = nullptr;
+  check(mcrg_alloc(&ctx, &cfg), "mcrg_alloc");
+  int rc = mcrg_sweep(ctx, n_eq);
+  if (rc == MCRG_OK) rc = mcrg_measure_flow(ctx, n_samples, 1, out);
+  mcrg_free(ctx);
+  if (rc != MCRG_OK) throw McrgError(rc, "mcrg_measure_flow");
+}
+
+}  // namespace
+
+double MonteCarloRenormalizationGroup::approx_critical_point(int n_samples_eq, int n_samples, int L, double K) {
+  if (L < 8 || (L & (L - 1))) throw McrgError(MCRG_EINVAL, "approx_critical_point: L");
+  const int n_transformations = (int)std::floor(std::log((double)L) / std::log((double)b_)) - 1;
+  mcrg_flow_moments mL, mS;
+  const uint64_t seed = seed_ + 1000003ull * (uint64_t)iter_;
+  printf("Sampling %i configurations each...\n", n_samples);
+  flow_of(L, K, seed, 0, device_, n_samples_eq, n_samples, &mL);
+  flow_of(L / b_, K, seed, 1, device_, n_samples_eq, n_samples, &mS);
+  const int64_t n = n_samples;
+  double Kc = 0.0;
+  kc_estimates_.clear();
+  for (int lev = 0; lev < n_transformations; ++lev) {
+    const long double dSL_dK = connected(mL.S0S[lev + 1], mL.S[lev + 1], mL.S[0], n);
+    const long double dSS_dK = connected(mS.S0S[lev], mS.S[lev], mS.S[0], n);
+    const long double dK = ((long double)(mL.S[lev + 1] - mS.S[lev]) / (long double)n) / (dSL_dK - dSS_dK);
+    Kc = (double)((long double)K + dK);
+    kc_estimates_.push_back(Kc);
+    printf("n = %i: Kc = %lf\n", lev, Kc);
+    if (fptr_) {
+      fprintf(fptr_, "%25i, %25i, %25.10lf, %25.10lf\n", iter_, lev, K, Kc);
+      fflush(fptr_);
+    }
+  }
+  return Kc;
+}
+
+double MonteCarloRenormalizationGroup::locate_critical_point(int n_iterations, int n_samples_eq, int n_samples,
+                                                            int L, double K0) {
+  printf("* Locating critical point starting from K0 = %lf\n", K0);
+  const std::string filename = "critical_point_L_" + std::to_string(L) + "_K_" + rounded(K0, 7) + ".txt";
+  fptr_ = fopen(filename.c_str(), "w");
+  if (fptr_) {
+    fprintf(fptr_, "# Number of parallel processes = %i\n", 1);
+    fprintf(fptr_, "# Number of equilibration samples = %i\n", n_samples_eq);
+    fprintf(fptr_, "# Number of samples = %i\n", n_samples);
+    fprintf(fptr_, "# %23s  %25s  %25s  %25s\n", "Iteration", "Blocking Level n", "Starting K", "Approximate Kc");
+  }
+  double K = K0;
+  try {
+    for (iter_ = 1; iter_ <= n_iterations; ++iter_) {
+      printf("\nIteration %i:\n", iter_);
+      K = approx_critical_point(n_samples_eq, n_samples, L, K);
+    }
+  } catch (...) {
+    if (fptr_) fclose(fptr_);
+    fptr_ = nullptr;
+    throw;
+  }
+  printf("\n* Critical point: Kc = %lf\n", K);
+  printf("* Critical temperature: Tc = %lf\n", -1.0 / K);
+  if (fptr_) fclose(fptr_);
+  fptr_ = nullptr;
+  return K;
+}

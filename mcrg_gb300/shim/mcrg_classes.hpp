@@ -111,10 +111,23 @@ class MonteCarloRenormalizationGroup {
   // src/mcrg.cpp:22-144: prints and writes critical_exponent_N_<N>_K_<K>.txt
   void calc_critical_exponent(int n_samples_eq, int n_samples, int N, double K);
 
+  // src/mcrg.cpp:145-189: iterated flow matching of lattices of side L and
+  // L/b; prints, writes critical_point_L_<L>_K_<K0>.txt, returns the last Kc
+  double locate_critical_point(int n_iterations, int n_samples_eq, int n_samples, int L, double K0);
+
+  // Kc estimate of every blocking level of the last matching iteration
+  std::vector<double> kc_estimates_;
+
   // results of the last calc_critical_exponent (one entry per level pair)
   std::vector<double> lambdas_;
   std::vector<double> nus_;
   uint64_t seed_ = 1;
   int n_couplings_ = 2;
   int device_ = 0;
+
+ private:
+  int iter_ = 0;
+  FILE* fptr_ = nullptr;
+  // src/mcrg.cpp:191-301: one matching step at K, returns the Kc of the largest level
+  double approx_critical_point(int n_samples_eq, int n_samples, int L, double K);
 };

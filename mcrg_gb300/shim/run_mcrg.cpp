@@ -1,12 +1,33 @@
 // run_mcrg -- the reference's src/main.cpp call sequence against the
 // GB300 library: MonteCarloRenormalizationGroup(b).calc_critical_exponent.
 // Usage: run_mcrg N n_eq n_samples K [seed] [n_couplings]
+//        run_mcrg locate L n_iterations n_eq n_samples K0 [seed]
+//          (MonteCarloRenormalizationGroup::locate_critical_point)
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 #include "mcrg_classes.hpp"
 
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "locate") {
+    const int L = argc > 2 ? atoi(argv[2]) : 16;
+    const int n_it = argc > 3 ? atoi(argv[3]) : 1;
+    const int n_eq = argc > 4 ? atoi(argv[4]) : 1000;
+    const int n_samples = argc > 5 ? atoi(argv[5]) : 10000;
+    const double K0 = argc > 6 ? atof(argv[6]) : -0.44;
+    try {
+      MonteCarloRenormalizationGroup MCRG(2);
+      if (argc > 7) MCRG.seed_ = strtoull(argv[7], nullptr, 10);
+      const double Kc = MCRG.locate_critical_point(n_it, n_eq, n_samples, L, K0);
+      for (size_t n = 0; n < MCRG.kc_estimates_.size(); ++n) printf("KC %zu %.12f\n", n, MCRG.kc_estimates_[n]);
+      printf("KCFINAL %.12f\n", Kc);
+    } catch (const McrgError& e) {
+      fprintf(stderr, "error: %s\n", e.what());
+      return 1;
+    }
+    return 0;
+  }
   int N = argc > 1 ? atoi(argv[1]) : 128;
   int n_eq = argc > 2 ? atoi(argv[2]) : 10000;
   int n_samples = argc > 3 ? atoi(argv[3]) : 1000000;

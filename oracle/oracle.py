@@ -199,5 +199,21 @@ def ref_lib() -> C.CDLL | None:
                                             P(C.c_double), C.c_int]
         h.ref_critical_exponent.restype = C.c_int
         h.ref_wolff.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_void_p]
+        h.ref_locate_critical_point.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                                C.c_char_p, P(C.c_double), C.c_int, P(C.c_double)]
+        h.ref_locate_critical_point.restype = C.c_int
         _ref = h
     return _ref
+
+
+def critical_point_estimates(SL: float, SS: float, SLb, SSb, SLbSL, SSbSS, K: float) -> list[float]:
+    """Restatement of the reference's matching step (src/mcrg.cpp:283-296) on sample
+    averages, in the reference's own double-precision order of operations:
+    dSL_dK = <SLb SL> - <SLb><SL>, dSS_dK likewise, dK = (<SLb> - <SSb>) / (dSL_dK - dSS_dK)."""
+    out = []
+    for n in range(len(SLb)):
+        dSL_dK = SLbSL[n] - SLb[n] * SL
+        dSS_dK = SSbSS[n] - SSb[n] * SS
+        dK = (SLb[n] - SSb[n]) / (dSL_dK - dSS_dK)
+        out.append(K + dK)
+    return out

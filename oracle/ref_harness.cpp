@@ -139,6 +139,35 @@ int ref_critical_exponent(uint64_t seed, int n_eq, int n_samples, int N, double 
     return got;
 }
 
+// Runs the reference's locate_critical_point (src/mcrg.cpp:145-189) in
+// directory `dir` after rng.seed(seed).  Writes the "Approximate Kc" column of
+// the critical_point_L_*.txt it produces (one row per iteration and level)
+// into kc, the returned K into *k_final, and returns the number of rows.
+int ref_locate_critical_point(uint64_t seed, int n_iterations, int n_eq, int n_samples, int L, double K0,
+                              const char* dir, double* kc, int max_rows, double* k_final) {
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return -1;
+    if (chdir(dir) != 0) return -2;
+    rng.seed(seed);
+    MonteCarloRenormalizationGroup mcrg(2);
+    *k_final = mcrg.locate_critical_point(n_iterations, n_eq, n_samples, L, K0);
+    std::string fn = "critical_point_L_" + std::to_string(L) + "_K_" + get_rounded_str(K0, 7) + ".txt";
+    FILE* f = fopen(fn.c_str(), "r");
+    int got = 0;
+    if (f) {
+        char line[512];
+        while (fgets(line, sizeof line, f)) {
+            if (line[0] == '#') continue;
+            int it, n;
+            double k, k_c;
+            if (sscanf(line, " %d , %d , %lf , %lf", &it, &n, &k, &k_c) == 4 && got < max_rows) kc[got++] = k_c;
+        }
+        fclose(f);
+    }
+    if (chdir(cwd) != 0) return -3;
+    return got;
+}
+
 // n Wolff steps of the reference (src/ising.cpp:87-149) on a lattice of side
 // N started from rng.seed(seed); returns the final lattice.
 void ref_wolff(uint64_t seed, int N, double K, int n_steps, int8_t* out) {

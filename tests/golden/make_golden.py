@@ -107,5 +107,29 @@ def main() -> None:
     print("reference lambda(L=8) mean", lams.mean(0), "std", lams.std(0, ddof=1))
 
 
+def main_critical():
+    """Kc estimates of the reference's locate_critical_point (src/mcrg.cpp:145-301):
+    one matching iteration from K0 = -0.44 per seed, every blocking level."""
+    R = O.ref_lib()
+    out = {}
+    for L, n_seeds in ((16, 16), (32, 8)):
+        n_eq, n_samples, K0 = 2000, 50000, -0.44
+        rows = []
+        for seed in range(1, n_seeds + 1):
+            kc = (C.c_double * 64)()
+            kf = C.c_double()
+            with tempfile.TemporaryDirectory() as td:
+                got = R.ref_locate_critical_point(seed, 1, n_eq, n_samples, L, K0, td.encode(), kc, 64, C.byref(kf))
+            rows.append(list(kc)[:got])
+        out["kc_L%d" % L] = np.array(rows)
+        out["n_eq_L%d" % L] = n_eq
+        out["n_samples_L%d" % L] = n_samples
+        print("reference Kc(L=%d) mean" % L, out["kc_L%d" % L].mean(0), "std", out["kc_L%d" % L].std(0, ddof=1))
+    np.savez_compressed(os.path.join(HERE, "ref_critical_point.npz"), K0=-0.44, **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["critical"]:
+        main_critical()
+    else:
+        main()
