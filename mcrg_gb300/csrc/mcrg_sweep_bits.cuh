@@ -39,6 +39,8 @@
 #include "mcrg_ops.cuh"
 #include "mcrg_tma.cuh"
 
+#include <type_traits>
+
 namespace mcrg {
 namespace bits {
 
@@ -189,8 +191,15 @@ struct Geo {
   static_assert(R >= 1, "one plane word per thread per group row");
 };
 
+// Lattice row of band row x: odd bands walk their rows bottom-up (ms = b0 +
+// b1 - 1 mirrors them, ms < 0 keeps them), so that the halo rows two
+// neighbouring bands share are read at about the same time (one DRAM read,
+// one L2 hit) instead of at opposite ends of the sweep.  The update is
+// symmetric in up / down, so only the row numbers change.
+__device__ __forceinline__ int lattice_row(int x, int ms, int L) { return ((ms >= 0 ? ms - x : x) + L) & (L - 1); }
+
 template <int NT, int LW, int LEAD>
-__device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, const uint8_t* in, uint8_t* raw,
+__device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, int ms, const uint8_t* in, uint8_t* raw,
                                             uint64_t* bar, int lane) {
   using G = Geo<NT, LW, LEAD>;
   const int x0 = top + g * G::R;
@@ -206,7 +215,7 @@ __device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, cons
     const bool want = c ? (x >= b0 - 2 && x <= b1 + 1) : (x >= b0 - 1 && x <= b1);
     if (want)
       tma::bulk_g2s(raw + ((size_t)c * G::RAW_ROWS + (x - top) % G::RAW_ROWS) * G::H,
-                    in + c * G::PLANE + (size_t)((x + G::L) & (G::L - 1)) * G::H, (uint32_t)G::H, br);
+                    in + c * G::PLANE + (size_t)lattice_row(x, ms, G::L) * G::H, (uint32_t)G::H, br);
   }
 }
 
@@ -215,7 +224,8 @@ __device__ __forceinline__ void issue_group(int g, int top, int b0, int b1, cons
 // shared memory (c = 0) or to the bytes already written to HBM (c = 1).
 template <int NT, int LW, int LEAD>
 __device__ __forceinline__ void resolve_queue(int c, int g, int first, int stride, const int* qn, const uint4* Q,
-                                              uint32_t* pk, uint8_t* out, int top, const Params& P, uint32_t tt) {
+                                              uint32_t* pk, uint8_t* out, int top, int ms, const Params& P,
+                                              uint32_t tt) {
   using G = Geo<NT, LW, LEAD>;
   constexpr int CAP = queue_cap<NT>();
   const int qi = c * 3 + g % 3;
@@ -223,7 +233,7 @@ __device__ __forceinline__ void resolve_queue(int c, int g, int first, int strid
   for (int e = first; e < n; e += stride) {
     const uint4 ent = Q[qi * CAP + e];
     const int off = (int)(ent.w >> 8), ww = (int)(ent.w & 0xFFu);
-    const int gr = (top + off + G::L) & (G::L - 1);
+    const int gr = lattice_row(top + off, ms, G::L);
     const uint32_t fl = open_flips(P, (uint32_t)c, gr, ww, ent.x, ent.y, tt);
     if (fl == 0u) continue;
     if (c == 0) {
@@ -265,38 +275,47 @@ __global__ void __launch_bounds__(NT, MINB)
   const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
   const int top = b0 - 2;
   const int J = (b1 - b0 + 4 + R - 1) / R;
+  const int ms = (blockIdx.x & 1) ? b0 + b1 - 1 : -1;
 
   if (tid < kRawSlots) tma::mbar_init(&bar[tid], 1);
   if (tid < 6) qn[tid] = 0;
   if (tid == 0) tma::fence_mbar_init();
   __syncthreads();
   if (tid < 32)
-    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, in, raw, bar, lane);
+    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, ms, in, raw, bar, lane);
 
+  // ok turns false when a bulk copy does not land in time; the phase's work
+  // then runs on stale shared memory (all indices stay in bounds) and the
+  // kernel reports the error at the phase barrier.  Keeping ok out of the
+  // work conditions leaves them uniform across each warp.
   bool ok = true;
-  for (int p = 0; p <= J + 5; ++p) {
+  // One phase; STEADY: every action of the phase is valid for every row (no
+  // band-edge checks).
+  auto phase = [&](int p, auto steady_tag) {
+    constexpr bool STEADY = decltype(steady_tag)::value;
     // queue lengths of buffers no phase touches now (read last phase, next appended after this one)
     if (tid == 0) {
-      if (p >= 4) qn[(p - 4) % 3] = 0;
-      if (p >= 7) qn[3 + (p - 7) % 3] = 0;
+      if (STEADY || p >= 4) qn[(p - 4) % 3] = 0;
+      if (STEADY || p >= 7) qn[3 + (p - 7) % 3] = 0;
     }
     // ---- open sites queued last phase: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6
     {
       const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
-      if (g >= 0 && g < J) resolve_queue<NT, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, P, tt);
+      if (STEADY || (g >= 0 && g < J))
+        resolve_queue<NT, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
     }
     // ---- bulk copies of group p + LEAD (its slot was packed last phase)
-    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, in, raw, bar, lane);
+    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
     // ---- pack group p
-    if (p < J) {
+    if (STEADY || p < J) {
       if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
       const int off = p * R + rr, x = top + off;
       const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
-      if (ok && x >= b0 - 1 && x <= b1) {
+      if (STEADY || (x >= b0 - 1 && x <= b1)) {
         const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
         pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
       }
-      if (ok && x <= b1 + 1) {
+      if (STEADY || x <= b1 + 1) {
         const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
         pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
       }
@@ -304,8 +323,8 @@ __global__ void __launch_bounds__(NT, MINB)
     // ---- colour 0 of group p-2
     {
       const int off = (p - 2) * R + rr, x = top + off;
-      if (ok && p >= 2 && p - 2 < J && x >= b0 - 1 && x <= b1) {
-        const int gr = (x + L) & (L - 1), pi = off & (PK_ROWS - 1);
+      if (STEADY || (p >= 2 && p - 2 < J && x >= b0 - 1 && x <= b1)) {
+        const int gr = lattice_row(x, ms, L), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk[pi * WPR + w];
         const uint32_t u = pk1[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t d = pk1[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
@@ -324,8 +343,8 @@ __global__ void __launch_bounds__(NT, MINB)
     // ---- colour 1 of group p-5, then both colours of its rows to the output
     {
       const int off = (p - 5) * R + rr, x = top + off;
-      if (ok && p >= 5 && p - 5 < J && x >= b0 && x <= b1 - 1) {
-        const int gr = (x + L) & (L - 1), pi = off & (PK_ROWS - 1);
+      if (STEADY || (p >= 5 && p - 5 < J && x >= b0 && x <= b1 - 1)) {
+        const int gr = lattice_row(x, ms, L), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk1[pi * WPR + w];
         const uint32_t u = pk[((pi - 1) & (PK_ROWS - 1)) * WPR + w];
         const uint32_t d = pk[((pi + 1) & (PK_ROWS - 1)) * WPR + w];
@@ -348,6 +367,17 @@ __global__ void __launch_bounds__(NT, MINB)
         o1[0] = a;
         o1[1] = b;
       }
+    }
+  };
+  // steady phases: groups p (pack), p-2, p-5 and the queues of p-3, p-6 all
+  // lie inside the band with every row valid
+  const int p_lo = 7;  // the colour-1 queue reset (group p-7) is the last action to become valid
+  const int p_hi = (b1 - b0 + 3 - R) / R;  // last phase whose pack group is all valid colour-0 rows
+  for (int p = 0; p <= J + 5; ++p) {
+    if (p >= p_lo && p <= p_hi) {
+      phase(p, std::true_type());
+    } else {
+      phase(p, std::false_type());
     }
     if (__syncthreads_or(!ok)) {
       // a copy did not land: wait (bounded) for the copies still in flight, then report
