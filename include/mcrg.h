@@ -29,8 +29,8 @@
  *   init   purpose 1, sub = colour, group = k>>7, time 0:
  *          spin bit = bit (k&127) of the 128-bit block;
  *   sweep  purpose 2, sub = colour, time = sweep index t; the 8-bit draw r8:
- *          L <= MCRG_SMEM_MAX_L: group = k>>4, r8 = byte (k&15);
- *          L >  MCRG_SMEM_MAX_L: groups 2w, 2w+1 with w = k>>5 give eight
+ *          L <= 32: group = k>>4, r8 = byte (k&15);
+ *          L >= 64: groups 2w, 2w+1 with w = k>>5 give eight
  *            plane words W0..W7; bit 7-q of r8 is bit 8*(p&3)+(p>>2) of Wq,
  *            p = k&31;
  *          purpose 3, group = k>>2: r24 = low 24 bits of word (k&3);
@@ -165,6 +165,14 @@ int mcrg_interactions(mcrg_ctx* ctx, int64_t* out);
  * q < n_bins_cap (binned error bars). */
 int mcrg_measure(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total,
                  int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap);
+
+/* Replaces RenormalizationGroupNeuralNetwork::scalar_output(spins_)
+ * (src/rgnn.cpp:281-307) on the current configuration, on the device: the 2x2
+ * filter out(i, j) = || W * block(2i, 2j, 2, 2) ||_1 applied until one value
+ * remains, W(r, k) = W[2r + k], FP64 in the reference's order of operations
+ * (same result bit for bit).  Does not move the chain or its counters, and
+ * spares the spins_ copy the reference's RGNN reads (src/rgnn.cpp:113-114). */
+int mcrg_rgnn_scalar_output(mcrg_ctx* ctx, const double W[4], double* out);
 
 /* Replaces the sample loop of approx_critical_point (src/mcrg.cpp:225-258)
  * for one of its two lattices: n_samples x (sweeps_between sweeps, then the

@@ -139,6 +139,15 @@ class Lattice:
         return FlowMoments(int(m.n_samples), [int(m.S[l]) for l in range(nl + 1)],
                            [_i128(m.S0S[l]) for l in range(nl + 1)])
 
+    def rgnn_scalar_output(self, W) -> float:
+        """RenormalizationGroupNeuralNetwork::scalar_output (src/rgnn.cpp:281-307) of the
+        current configuration, on the device; W is the 2x2 weight matrix."""
+        w = np.asarray(W, dtype=np.float64).reshape(4)
+        out = C.c_double()
+        check(lib().mcrg_rgnn_scalar_output(self._ctx, (C.c_double * 4)(*w), C.byref(out)),
+              "mcrg_rgnn_scalar_output")
+        return float(out.value)
+
     def counters(self) -> tuple[int, int]:
         t = C.c_uint64()
         n = C.c_uint64()
@@ -169,7 +178,14 @@ class IsingModel:
         self.P_ = 1.0 - math.exp(2.0 * K)  # kept for API parity (Wolff bond probability)
 
     def equilibrate(self, lattice: Lattice, n_samples_eq: int, write: bool = False) -> None:
-        lattice.sweep(n_samples_eq)
+        """src/ising.cpp:14-84; with write, logs equilibrate_N_<N>_K_<K>.txt in the
+        reference's format (see mcrg_gb300.logfiles)."""
+        if not write:
+            lattice.sweep(n_samples_eq)
+            return
+        from .logfiles import write_equilibrate
+
+        write_equilibrate(self, lattice, n_samples_eq)
 
     def sample_new_configuration(self, lattice: Lattice) -> None:
         lattice.sweep(1)

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmcrg.so")
-UNITS = ["mcrg_chain.cu", "mcrg_tiled.cu", "mcrg_capi.cu", "mcrg_batch.cu", "mcrg_noalloc.cu"]
+UNITS = ["mcrg_chain.cu", "mcrg_tiled.cu", "mcrg_capi.cu", "mcrg_batch.cu", "mcrg_noalloc.cu", "mcrg_rgnn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                      "--expt-relaxed-constexpr"]
@@ -81,7 +81,8 @@ def build_shim(force: bool = False) -> str:
                                                       for d in deps):
         return SHIM_BIN
     tmp = SHIM_BIN + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O2", "-std=c++17"] + srcs + ["-L", OUT_DIR, "-lmcrg", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    # no FMA contraction: the log files reproduce the reference's double arithmetic
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off"] + srcs + ["-L", OUT_DIR, "-lmcrg", "-Wl,-rpath,$ORIGIN", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("shim build failed:\n%s%s" % (r.stdout, r.stderr))

@@ -33,6 +33,7 @@ struct mcrg_ctx {
   int8_t* d_nat = nullptr;      // natural-layout staging (L*L)
   int* d_flag = nullptr;
   Accept acc;
+  double* d_rgnn = nullptr;     // forward-pass work: (L/32)^2 + (L/1024)^2 + 3 doubles, the last one the result
 };
 
 namespace {
@@ -279,6 +280,7 @@ int mcrg_free(mcrg_ctx* c) {
   cudaFree(c->d_bins);
   cudaFree(c->d_nat);
   cudaFree(c->d_flag);
+  cudaFree(c->d_rgnn);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MCRG_OK;
@@ -566,3 +568,17 @@ int mcrg_lattice_couplings(int32_t N, const int8_t* host_in, int32_t n_couplings
 }
 
 }  // extern "C"
+
+int mcrg_rgnn_scalar_output(mcrg_ctx* c, const double* W, double* out) {
+  if (!c || !W || !out) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int L = c->cfg.L;
+  const size_t nwork = (size_t)(L / 32) * (L / 32) + (size_t)(L / 1024) * (L / 1024) + 3;
+  if (!c->d_rgnn && cudaMalloc(&c->d_rgnn, sizeof(double) * nwork) != cudaSuccess) return MCRG_ENOMEM;
+  const uint8_t* state = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  double* d_out = c->d_rgnn + nwork - 1;
+  CK(launch_rgnn_scalar(state, L, W, c->d_rgnn, d_out, c->stream));
+  CK(cudaMemcpyAsync(out, d_out, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return MCRG_OK;
+}

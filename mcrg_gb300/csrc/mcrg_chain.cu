@@ -9,7 +9,9 @@
 // between the initial load and the final store except the per-bin moment
 // flushes.
 //
-// Sweep: the 16 sites of a 16-byte chunk of one colour row are updated with
+// Sweep (L >= 64): bit-sliced on a plane-word copy of level 0
+// (mcrg_resident_bits.cuh), the bytes refreshed before each measurement.
+// Sweep (L <= 32): the 16 sites of a 16-byte chunk of one colour row are updated with
 // byte-SWAR arithmetic from one Philox block (one 8-bit draw per site).  A
 // site whose 8-bit draw equals the top byte of its threshold is left open and
 // queued; after the colour's pass the queue is resolved exactly with the
@@ -17,6 +19,7 @@
 // interact, so resolving them after the pass gives the same result as
 // resolving them in place.
 #include "mcrg_ops.cuh"
+#include "mcrg_resident_bits.cuh"
 
 namespace mcrg {
 
@@ -54,6 +57,11 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   const int E = J.flow ? 2 * (nl + 1) : plan.E;
   uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (threadIdx.x >> 5) * kOpenPerWarp;
   const bool vec = acc.fast && L >= 16;
+  // L >= 64 in the fast regime: sweeps run on a plane-word copy of level 0
+  const bool bits = acc.fast && L >= 64;
+  uint32_t* pl = bits ? reinterpret_cast<uint32_t*>(smem + plan.pl_off) : nullptr;
+  int* qn = bits ? reinterpret_cast<int*>(smem + plan.pl_off + 2 * (L * L / 64) * 4) : nullptr;
+  uint4* oq = bits ? reinterpret_cast<uint4*>(smem + plan.q_off) : nullptr;
 
   // ---- configuration into shared memory
   if (J.init) {
@@ -88,12 +96,27 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
     tab[e] = make_int2(x | (y << 16), out);
     macc[e] = 0;
   }
+  if (bits && tid < 2) qn[tid] = 0;
   __syncthreads();
+  if (bits) {
+    resident::pack_lattice(lat, pl, L, tid, T);
+    __syncthreads();
+  }
 
   uint32_t t = J.t0;
-  for (int64_t s = 0; s < J.n_eq; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
+  for (int64_t s = 0; s < J.n_eq; ++s) {
+    if (bits) resident::sweep(pl, L, t++, key, rep, acc, tid, T, oq, qn);
+    else chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
+  }
   for (int64_t n = 0; n < J.n_samples; ++n) {
-    for (int64_t s = 0; s < J.sweeps_between; ++s) chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
+    for (int64_t s = 0; s < J.sweeps_between; ++s) {
+      if (bits) resident::sweep(pl, L, t++, key, rep, acc, tid, T, oq, qn);
+      else chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
+    }
+    if (bits) {  // the measurement reads the byte lattice
+      resident::unpack_lattice(pl, lat, L, tid, T);
+      __syncthreads();
+    }
     // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
@@ -148,6 +171,10 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   }
 
   // ---- final configuration back to HBM
+  if (bits) {
+    resident::unpack_lattice(pl, lat, L, tid, T);
+    __syncthreads();
+  }
   if (J.store) {
     const uint4* src = reinterpret_cast<const uint4*>(lat);
     uint4* dst = reinterpret_cast<uint4*>(J.state);

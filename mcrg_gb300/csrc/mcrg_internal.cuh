@@ -36,6 +36,8 @@ struct SmemPlan {
   int scr_off;  // uint32 open-site scratch: 64 per warp, up to 8 warps
   int E;        // moment entries of the T-matrix moments
   int Ecap;     // entries the table holds (also fits the 2 (n_levels + 1) flow moments)
+  int pl_off;   // L >= 64: plane words of level 0 (2 L^2 / 64 uint32), then qn[2] and the open-word queue
+  int q_off;    // uint4 queue entries (resident::queue_cap(L))
   int bytes;
 };
 
@@ -56,6 +58,14 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
   off += p.Ecap * 8;
   p.scr_off = off;
   off += 8 * 64 * 4;
+  p.pl_off = p.q_off = -1;
+  if (L >= 64) {  // bit-sliced sweeps (mcrg_resident_bits.cuh)
+    off = (off + 15) / 16 * 16;
+    p.pl_off = off;
+    off += 2 * (L * L / 64) * 4 + 16;  // planes + qn[2] (padded)
+    p.q_off = off;
+    off += (L * L / 256 > 32 ? L * L / 256 : 32) * 16;
+  }
   p.bytes = (off + 15) / 16 * 16;
   return p;
 }
@@ -75,5 +85,11 @@ cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels
 cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat,
                               Key key, uint32_t replica, int level, uint32_t sample, cudaStream_t s);
 cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out, cudaStream_t s);
+
+// Forward pass of the RG neural network (src/rgnn.cpp:281-307) on a split
+// layout lattice of side n: the scalar output into *d_out (device), using
+// `work` ((n/32)^2 + (n/1024)^2 + 2 doubles, not overlapping d_out).
+cudaError_t launch_rgnn_scalar(const uint8_t* d_split, int n, const double W[4], double* work, double* d_out,
+                               cudaStream_t s);
 
 }  // namespace mcrg

@@ -221,7 +221,9 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
   }
 }
 
-// Scalar sweep of colour c (any n >= 4, any K): exact 32-bit draw per site.
+// Scalar sweep of colour c (any n >= 4, any K): exact 32-bit draw per site;
+// the 8-bit part r8 comes from bytes for n <= 32 and from bit planes for
+// n >= 64 (the layouts of the byte-SWAR and bit-sliced sweeps).
 __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
                                     const Accept& a, int tid, int T) {
   const int half = n / 2;
@@ -238,9 +240,20 @@ __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key 
     if ((a.always_mask >> m) & 1u) {
       flip = true;
     } else {
-      const uint4 hi = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 4), t);
+      uint32_t r8;
+      if (n >= 64) {  // bit-plane draws (groups 2w, 2w+1; bit 7-q of r8 = plane bit of word q)
+        const int w = k >> 5, p = k & 31, pos = 8 * (p & 3) + (p >> 2);
+        const uint4 A = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w), t);
+        const uint4 B = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w + 1), t);
+        const uint32_t W[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+        r8 = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) r8 |= ((W[q] >> pos) & 1u) << (7 - q);
+      } else {  // byte draws
+        const uint4 hi = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 4), t);
+        r8 = (u4get(hi, (k & 15) >> 2) >> (8 * (k & 3))) & 0xFFu;
+      }
       const uint4 lo = stream_block(key, rep, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
-      const uint32_t r8 = (u4get(hi, (k & 15) >> 2) >> (8 * (k & 3))) & 0xFFu;
       const uint32_t u32 = (r8 << 24) | (u4get(lo, k & 3) & 0xFFFFFFu);
       flip = u32 < a.thr[m];
     }

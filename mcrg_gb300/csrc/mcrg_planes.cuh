@@ -1,0 +1,67 @@
+// mcrg_planes.cuh -- bit-plane words of a colour row and the bit-sliced
+// Metropolis decision, shared by the HBM sweep (mcrg_sweep_bits.cuh) and the
+// shared-memory-resident chains (mcrg_chain.cu).
+//
+// 32 consecutive sites k = 32w .. 32w+31 of one colour row form plane word w;
+// site k = 32w + p sits at bit pos(p) = 8*(p&3) + (p>>2).  That order makes
+// packing 32 int8 sites (bytes 0/1) a sum of eight shifted 32-bit loads and
+// unpacking eight shift-and-mask pairs.  The eight random planes of a word are
+// the words of its two P_SWEEP_HI Philox blocks (groups 2w, 2w+1): bit pos(p)
+// of plane q is bit 7-q of the site's 8-bit draw r8.
+#pragma once
+#include <cstdint>
+
+namespace mcrg {
+namespace planes {
+
+// plane bit of site p (0..31) of a word, and its inverse
+__device__ __forceinline__ int plane_pos(int p) { return 8 * (p & 3) + (p >> 2); }
+__device__ __forceinline__ int plane_site(int pos) { return 4 * (pos & 7) + (pos >> 3); }
+
+// 32 sites (bytes 0/1, a = bytes 0..15, b = bytes 16..31) -> plane word
+__device__ __forceinline__ uint32_t pack_bytes(const uint4& a, const uint4& b) {
+  return a.x + (a.y << 1) + (a.z << 2) + (a.w << 3) + (b.x << 4) + (b.y << 5) + (b.z << 6) + (b.w << 7);
+}
+
+__device__ __forceinline__ void unpack_bytes(uint32_t x, uint4& a, uint4& b) {
+  const uint32_t M = 0x01010101u;
+  a = make_uint4(x & M, (x >> 1) & M, (x >> 2) & M, (x >> 3) & M);
+  b = make_uint4((x >> 4) & M, (x >> 5) & M, (x >> 6) & M, (x >> 7) & M);
+}
+
+// Word of the sites k+1 (right) / k-1 (left) of every site k of word x;
+// xn / xp is the next / previous word of the row.
+__device__ __forceinline__ uint32_t right_sites(uint32_t x, uint32_t xn) {
+  return (x >> 8) | ((x << 23) & 0x7F000000u) | (xn << 31);
+}
+__device__ __forceinline__ uint32_t left_sites(uint32_t x, uint32_t xp) {
+  return (x << 8) | ((x >> 23) & 0xFEu) | (xp >> 31);
+}
+
+// Bit-sliced update of 32 sites t from their neighbours u, d (other colour,
+// rows above and below), mid (same byte index) and side (the other
+// horizontal neighbour).  tz / to: the top bytes of thr[0] / thr[1] as
+// all-ones / all-zero masks per plane (plane 0 = most significant bit).
+// Returns the new word; `open` gets the sites whose draw ties the
+// threshold's top byte, `zero` the sites with m = 0.
+__device__ __forceinline__ uint32_t decide(uint32_t t, uint32_t u, uint32_t d, uint32_t mid, uint32_t side,
+                                           const uint4& A, const uint4& B, const uint32_t (&tz)[8],
+                                           const uint32_t (&to)[8], uint32_t& open, uint32_t& zero) {
+  const uint32_t s1 = (u ^ t) | (d ^ t), p1 = (u ^ t) & (d ^ t);
+  const uint32_t s2 = (mid ^ t) | (side ^ t), p2 = (mid ^ t) & (side ^ t);
+  const uint32_t ge2 = p1 | p2 | (s1 & s2);  // m >= 2: always flips
+  zero = ~(s1 | s2);
+  const uint32_t W[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+  uint32_t br = 0u, eq = ~0u;  // borrow of r8 - T8 (r8 < T8), r8 == T8
+#pragma unroll
+  for (int q = 7; q >= 0; --q) {
+    const uint32_t th = (zero & tz[q]) | (~zero & to[q]);
+    br = (~W[q] & (th | br)) | (th & br);
+    eq &= ~(W[q] ^ th);
+  }
+  open = eq & ~ge2;
+  return t ^ (ge2 | br);
+}
+
+}  // namespace planes
+}  // namespace mcrg

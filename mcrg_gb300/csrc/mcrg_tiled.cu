@@ -277,23 +277,30 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // two rounds of 20 launches per variant, best round kept: the leading
+  // variants differ by ~1 %, below the spread of a single short round
   int best = -1;
   float best_ms = 1e30f;
-  const int reps = 10;
-  for (int v = 0; v < kNumVariants; ++v) {
-    if (!variant_fits(kVariants[v], t->L)) continue;
-    launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u, s);  // warm-up
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < reps; ++r) launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u + r, s);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) {
-      best_ms = ms;
+  float round_best[kNumVariants];
+  for (int v = 0; v < kNumVariants; ++v) round_best[v] = 1e30f;
+  const int reps = 20;
+  for (int round = 0; round < 2; ++round)
+    for (int v = 0; v < kNumVariants; ++v) {
+      if (!variant_fits(kVariants[v], t->L)) continue;
+      launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u, s);  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < reps; ++r) launch_variant(t, v, t->buf[t->cur], t->buf[t->cur ^ 1], 0xFFFFFFF0u + r, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < round_best[v]) round_best[v] = ms;
+    }
+  for (int v = 0; v < kNumVariants; ++v)
+    if (round_best[v] < best_ms) {
+      best_ms = round_best[v];
       best = v;
     }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) return -1;

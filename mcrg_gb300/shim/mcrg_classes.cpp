@@ -82,9 +82,84 @@ double Lattice::calc_nearest_neighbor_interaction() { return calc_interactions()
 
 IsingModel::IsingModel(double K) : K_(K), P_(1.0 - std::exp(2.0 * K)) {}
 
-void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool /*write*/) {
-  check(mcrg_sweep(p->ctx(), n_samples_eq), "mcrg_sweep");
-  p->refresh();
+namespace {
+
+// the reference's write_iter (src/definitions.cpp:44-68): logged iterations
+bool write_iter(int i) {
+  if (i < 10) return true;
+  if (i < 100) return i % 10 == 0;
+  if (i < 1000) return i % 100 == 0;
+  if (i < 10000) return i % 1000 == 0;
+  if (i < 100000) return i % 10000 == 0;
+  return i % 100000 == 0;
+}
+
+// S_nn of a +-1 matrix (each bond counted twice, src/lattice.cpp:102-120)
+long long nn_sum(const SpinMatrix& s) {
+  const int N = s.rows();
+  long long S = 0;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j)
+      S += (long long)s(i, j) * (s((i + 1) % N, j) + s((i + N - 1) % N, j) + s(i, (j + 1) % N) + s(i, (j + N - 1) % N));
+  return S;
+}
+
+}  // namespace
+
+// src/ising.cpp:14-84.  The sweeps between two logged iterations run in one
+// device call (the chain is the same as sweeping one by one).  The logged
+// columns follow the reference's arithmetic with one process: E = K S_nn / N^2
+// (calc_energy) divided again by the number of sites, |M| from the integer
+// division of calc_magnetization (src/ising.cpp:176-179), spreads over the
+// processes (zero here).
+void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool write) {
+  if (!write) {
+    check(mcrg_sweep(p->ctx(), n_samples_eq), "mcrg_sweep");
+    p->refresh();
+    return;
+  }
+  const std::string filename = "equilibrate_N_" + std::to_string(p->N_) + "_K_" + rounded(K_, 7) + ".txt";
+  FILE* f = fopen(filename.c_str(), "w");
+  if (!f) throw McrgError(MCRG_EIO, "equilibrate: cannot open the output file");
+  fprintf(f, "# Nearest neighbor coupling K = %lf\n", K_);
+  fprintf(f, "# Temperature T = %lf\n", -1 / K_);
+  fprintf(f, "# Number of lattice sites = %i\n", p->N_ * p->N_);
+  fprintf(f, "# Lattice spacing = %i\n", p->a_);
+  fprintf(f, "# Using %i parallel processes\n", 1);
+  fprintf(f, "# %s, %s, %s, %s, %s, %s, %s\n", "Iteration", "Avg E/spin", "Stddev E/spin", "Heat Capacity",
+          "Avg |M|/spin", "Stddev |M|/spin", "Susceptibility");
+  int done = 0;
+  try {
+    for (int n = 1; n <= n_samples_eq; ++n) {
+      if (!write_iter(n)) continue;
+      check(mcrg_sweep(p->ctx(), n - done), "mcrg_sweep");
+      done = n;
+      p->sync_spins();
+      const int NN = p->N_ * p->N_;
+      const double E = K_ * (double)nn_sum(p->spins_) / NN;
+      const double M = std::abs((double)(int)(p->spins_.sum() / NN));
+      const double E2 = E * E, M2 = M * M;
+      double E_sigma = E2 - E * E, M_sigma = M2 - M * M;
+      const double C = E_sigma * K_ * K_, Chi = -M_sigma * K_;
+      E_sigma = std::sqrt(E_sigma);
+      M_sigma = std::sqrt(M_sigma);
+      fprintf(f, "%i, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e\n", n, E / p->n_spins_, E_sigma / p->n_spins_, C,
+              M / p->n_spins_, M_sigma / p->n_spins_, Chi);
+    }
+    if (done < n_samples_eq) check(mcrg_sweep(p->ctx(), n_samples_eq - done), "mcrg_sweep");
+  } catch (...) {
+    fclose(f);
+    throw;
+  }
+  p->sync_spins();
+  // Lattice::write_spins (src/lattice.cpp:63-75)
+  fprintf(f, "\n");
+  for (int i = 0; i < p->N_; ++i) {
+    fprintf(f, "# ");
+    for (int j = 0; j < p->N_; ++j) fprintf(f, "%i, ", p->spins_(i, j));
+    fprintf(f, "\n");
+  }
+  fclose(f);
 }
 
 void IsingModel::sample_new_configuration(std::shared_ptr<Lattice> p) {
@@ -243,4 +318,10 @@ double MonteCarloRenormalizationGroup::locate_critical_point(int n_iterations, i
   if (fptr_) fclose(fptr_);
   fptr_ = nullptr;
   return K;
+}
+
+double Lattice::rgnn_scalar_output(const double W[4]) const {
+  double out = 0.0;
+  check(mcrg_rgnn_scalar_output(ctx_, W, &out), "mcrg_rgnn_scalar_output");
+  return out;
 }

@@ -78,6 +78,10 @@ class Lattice {
   void upload_spins();
   void sync_spins();
 
+  // RenormalizationGroupNeuralNetwork::scalar_output(spins_) (src/rgnn.cpp:281-307)
+  // on the device, W(r, k) = W[2r + k]
+  double rgnn_scalar_output(const double W[4]) const;
+
   mcrg_ctx* ctx() const { return ctx_; }
   void refresh() {
     if (mirror_spins_) sync_spins();

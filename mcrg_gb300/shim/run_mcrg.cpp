@@ -3,13 +3,43 @@
 // Usage: run_mcrg N n_eq n_samples K [seed] [n_couplings]
 //        run_mcrg locate L n_iterations n_eq n_samples K0 [seed]
 //          (MonteCarloRenormalizationGroup::locate_critical_point)
+//        run_mcrg rgnn N seed W00 W01 W10 W11  (Lattice::rgnn_scalar_output of the initial coin)
+//        run_mcrg equilibrate N n K [seed]
+//          (IsingModel::equilibrate(lattice, n, true): writes equilibrate_N_*.txt)
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <string>
 
 #include "mcrg_classes.hpp"
 
 int main(int argc, char** argv) {
+  if (argc > 7 && std::string(argv[1]) == "rgnn") {
+    try {
+      Lattice lat(atoi(argv[2]), -0.44068679350977147, strtoull(argv[3], nullptr, 10));
+      const double W[4] = {atof(argv[4]), atof(argv[5]), atof(argv[6]), atof(argv[7])};
+      printf("RGNN %.17g\n", lat.rgnn_scalar_output(W));
+    } catch (const McrgError& e) {
+      fprintf(stderr, "error: %s\n", e.what());
+      return 1;
+    }
+    return 0;
+  }
+  if (argc > 1 && std::string(argv[1]) == "equilibrate") {
+    const int N = argc > 2 ? atoi(argv[2]) : 8;
+    const int n = argc > 3 ? atoi(argv[3]) : 1000;
+    const double K = argc > 4 ? atof(argv[4]) : -0.44068679350977147;
+    const uint64_t seed = argc > 5 ? strtoull(argv[5], nullptr, 10) : 1;
+    try {
+      std::shared_ptr<Lattice> lat(new Lattice(N, K, seed));
+      IsingModel model(K);
+      model.equilibrate(lat, n, true);
+    } catch (const McrgError& e) {
+      fprintf(stderr, "error: %s\n", e.what());
+      return 1;
+    }
+    return 0;
+  }
   if (argc > 1 && std::string(argv[1]) == "locate") {
     const int L = argc > 2 ? atoi(argv[2]) : 16;
     const int n_it = argc > 3 ? atoi(argv[3]) : 1;

@@ -4,7 +4,7 @@
   ``oracle/_build/liboracle.so`` (gcc, portable flags: it must build the same
   on x86-64 and aarch64).
 * ``build_ref()`` compiles the reference's own unmodified sources
-  (src/definitions.cpp, lattice.cpp, ising.cpp, mcrg.cpp of kim-jane/MCRG,
+  (src/definitions.cpp, lattice.cpp, ising.cpp, mcrg.cpp, rgnn.cpp of kim-jane/MCRG,
   read where they lie under ``/root/reference``) together with
   ``oracle/ref_harness.cpp`` and the single-rank ``oracle/stub_mpi/mpi.h``
   into ``oracle/_ref/libmcrg_ref.so``.  Nothing is copied out of the
@@ -48,7 +48,7 @@ def ref_available() -> bool:
 def build_ref(force: bool = False) -> str | None:
     if not ref_available():
         return None
-    units = [os.path.join(REF_SRC, f) for f in ("definitions.cpp", "lattice.cpp", "ising.cpp", "mcrg.cpp")]
+    units = [os.path.join(REF_SRC, f) for f in ("definitions.cpp", "lattice.cpp", "ising.cpp", "mcrg.cpp", "rgnn.cpp")]
     harness = os.path.join(HERE, "ref_harness.cpp")
     if not force and _newer(REF_SO, units + [harness]):
         return REF_SO

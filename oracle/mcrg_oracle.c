@@ -112,11 +112,11 @@ void orc_init_spins(int N, uint64_t seed, uint32_t replica, int8_t* s) {
 /* Checkerboard Metropolis sweep (black (i+j even) then white).         */
 /* Site (i, j) of colour c = (i+j)&1 is byte k = j>>1 of its colour     */
 /* row.  Site random u32 = r8 << 24 | r24 where r8 depends on N:        */
-/*   N <= ORC_SMEM_MAX_L (byte draws):                                  */
+/*   N <  ORC_PLANE_MIN_L (byte draws):                                 */
 /*     r8 = byte (k&15) of the P_SWEEP_HI block (row i, group k>>4,     */
 /*          sub = colour c, time = sweep t); byte b of a block is byte  */
 /*          (b&3) of word (b>>2), little-endian;                        */
-/*   N >  ORC_SMEM_MAX_L (bit-plane draws, 32 sites per plane word):    */
+/*   N >= ORC_PLANE_MIN_L (bit-plane draws, 32 sites per plane word):   */
 /*     with w = k>>5, p = k&31 and pos = 8*(p&3) + (p>>2), the planes   */
 /*     W0..W7 are the words of the P_SWEEP_HI blocks (row i, group 2w   */
 /*     and 2w+1, sub = c, time = t) in order, and bit 7-q of r8 is bit  */
@@ -125,7 +125,7 @@ void orc_init_spins(int N, uint64_t seed, uint32_t replica, int8_t* s) {
 /*         (row i, group k>>2, sub = c, time = t), both layouts.        */
 /* Flip iff always[m] or u32 < thr[m].                                  */
 /* ------------------------------------------------------------------ */
-#define ORC_SMEM_MAX_L 256
+#define ORC_PLANE_MIN_L 64   /* one colour row holds whole plane words */
 
 static uint32_t plane_r8(const uint32_t planes[8], int k) {
     int p = k & 31, pos = 8 * (p & 3) + (p >> 2);
@@ -138,7 +138,7 @@ void orc_sweep(int N, int8_t* s, double K, uint64_t seed, uint32_t replica,
     uint32_t thr[5]; uint8_t always[5];
     orc_thresholds(K, thr, always);
     uint32_t hi[4], lo[4], planes[8];
-    const int bit_planes = N > ORC_SMEM_MAX_L;
+    const int bit_planes = N >= ORC_PLANE_MIN_L;
     for (int64_t n = 0; n < n_sweeps; ++n) {
         uint32_t t = t0 + (uint32_t)n;
         for (int c = 0; c < 2; ++c)

@@ -202,6 +202,10 @@ def ref_lib() -> C.CDLL | None:
         h.ref_locate_critical_point.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                                 C.c_char_p, P(C.c_double), C.c_int, P(C.c_double)]
         h.ref_locate_critical_point.restype = C.c_int
+        h.ref_equilibrate_log.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_char_p]
+        h.ref_equilibrate_log.restype = C.c_int
+        h.ref_rgnn_scalar_output.argtypes = [C.c_int, C.c_void_p, P(C.c_double)]
+        h.ref_rgnn_scalar_output.restype = C.c_double
         _ref = h
     return _ref
 
@@ -217,3 +221,21 @@ def critical_point_estimates(SL: float, SS: float, SLb, SSb, SLbSL, SSbSS, K: fl
         dK = (SLb[n] - SSb[n]) / (dSL_dK - dSS_dK)
         out.append(K + dK)
     return out
+
+
+def rgnn_scalar_output(spins: np.ndarray, W) -> float:
+    """Restatement of RenormalizationGroupNeuralNetwork::scalar_output
+    (src/rgnn.cpp:281-307): apply the 2x2 filter until one value remains,
+    out(i, j) = || W * block(2i, 2j, 2, 2) ||_1, with the reference's floating-point
+    order: conv(r, c) = W(r, 0) B(0, c) + W(r, 1) B(1, c) (no fused multiply-add),
+    L1 = (|c00| + |c01|) + (|c10| + |c11|)."""
+    W = np.asarray(W, dtype=np.float64).reshape(2, 2)
+    v = np.asarray(spins, dtype=np.float64)
+    while v.shape[0] > 1:
+        B00, B01, B10, B11 = v[0::2, 0::2], v[0::2, 1::2], v[1::2, 0::2], v[1::2, 1::2]
+        c00 = W[0, 0] * B00 + W[0, 1] * B10
+        c01 = W[0, 0] * B01 + W[0, 1] * B11
+        c10 = W[1, 0] * B00 + W[1, 1] * B10
+        c11 = W[1, 0] * B01 + W[1, 1] * B11
+        v = (np.abs(c00) + np.abs(c01)) + (np.abs(c10) + np.abs(c11))
+    return float(v[0, 0])

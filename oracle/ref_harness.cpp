@@ -15,6 +15,7 @@
 #include <unistd.h>
 #define private public       // reach MonteCarloRenormalizationGroup::block_spin_transformation
 #include "mcrg.hpp"
+#include "rgnn.hpp"
 #undef private
 
 namespace {
@@ -166,6 +167,36 @@ int ref_locate_critical_point(uint64_t seed, int n_iterations, int n_eq, int n_s
     }
     if (chdir(cwd) != 0) return -3;
     return got;
+}
+
+// Runs the reference's IsingModel::equilibrate(lattice, n, true)
+// (src/ising.cpp:14-84) in directory `dir` after rng.seed(seed); it writes
+// equilibrate_N_<N>_K_<K>.txt there.  Returns 0.
+int ref_equilibrate_log(uint64_t seed, int N, double K, int n, const char* dir) {
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd)) return -1;
+    if (chdir(dir) != 0) return -2;
+    rng.seed(seed);
+    IsingModel m(K);
+    std::shared_ptr<Lattice> lat(new Lattice(N));
+    m.equilibrate(lat, n, true);
+    if (chdir(cwd) != 0) return -3;
+    return 0;
+}
+
+// RenormalizationGroupNeuralNetwork::scalar_output (src/rgnn.cpp:281-307)
+// of a +-1 lattice (row-major, site (i, j) at i*N + j = spins_(i, j)) with
+// weights W(r, k) = W[2r + k].
+double ref_rgnn_scalar_output(int N, const int8_t* spins, const double* W) {
+    imat s(N, N);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) s(i, j) = spins[i * N + j];
+    RenormalizationGroupNeuralNetwork net(2);
+    mat w(2, 2);
+    for (int r = 0; r < 2; ++r)
+        for (int k = 0; k < 2; ++k) w(r, k) = W[2 * r + k];
+    net.set_weights(w);
+    return net.scalar_output(s);
 }
 
 // n Wolff steps of the reference (src/ising.cpp:87-149) on a lattice of side

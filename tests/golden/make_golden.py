@@ -128,8 +128,42 @@ def main_critical():
     np.savez_compressed(os.path.join(HERE, "ref_critical_point.npz"), K0=-0.44, **out)
 
 
+def main_equilibrate():
+    """The file the reference's IsingModel::equilibrate(lat, n, true) writes (src/ising.cpp:14-84)."""
+    R = O.ref_lib()
+    with tempfile.TemporaryDirectory() as td:
+        rc = R.ref_equilibrate_log(5, 8, KC, 250, td.encode())
+        assert rc == 0
+        fn = os.path.join(td, "equilibrate_N_8_K_-0.4406868.txt")
+        text = open(fn).read()
+    with open(os.path.join(HERE, "ref_equilibrate_N_8.txt"), "w") as f:
+        f.write(text)
+    print(text[:400])
+
+
+def main_rgnn():
+    """RenormalizationGroupNeuralNetwork::scalar_output (src/rgnn.cpp:281-307) of the
+    reference on seeded +-1 lattices and weights."""
+    R = O.ref_lib()
+    rng = np.random.default_rng(2024)
+    sizes, spins, Ws, outs = [], [], [], []
+    for N in (2, 4, 8, 16, 32, 64, 128, 256):
+        for t in range(3):
+            s = np.where(rng.random((N, N)) < (0.5 if t < 2 else 0.9), 1, -1).astype(np.int8)
+            W = rng.normal(size=(2, 2))
+            sizes.append(N); spins.append(s.ravel()); Ws.append(W.ravel())
+            outs.append(R.ref_rgnn_scalar_output(N, s.ctypes.data, (C.c_double * 4)(*W.ravel())))
+    np.savez_compressed(os.path.join(HERE, "ref_rgnn.npz"), sizes=np.array(sizes), spins=np.concatenate(spins),
+                        W=np.array(Ws), out=np.array(outs))
+    print("rgnn outputs", outs[:6])
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["critical"]:
+    if sys.argv[1:] == ["rgnn"]:
+        main_rgnn()
+    elif sys.argv[1:] == ["critical"]:
         main_critical()
+    elif sys.argv[1:] == ["equilibrate"]:
+        main_equilibrate()
     else:
         main()
