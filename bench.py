@@ -305,7 +305,7 @@ def run_plain_subset(M, reqs, device) -> dict:
         lat.measure(r.n_samples, r.sweeps_between)
         lat.close()
     dt = time.perf_counter() - t0
-    flips = float(sum(r.L * r.L for r in reqs)) * reqs[0].n_samples
+    flips = float(sum(r.L * r.L * (r.n_eq + r.n_samples * r.sweeps_between) for r in reqs))
     return {"solves_per_s": round(len(reqs) / dt, 2), "Gflips_per_s": round(flips / dt / 1e9, 3),
             "requests": len(reqs), "seconds": round(dt, 3)}
 
@@ -374,7 +374,11 @@ def run_served(args, D: Dist) -> dict:
         srv.close()
     lat = np.array(lat)
     flips = float(sum(int(L) * int(L) * int(s) for L, s in zip(Ls, sw)))
+    # the plain GPU path on a random subset of the same requests (one lattice per launch, back to back)
+    sub = [reqs[int(i)] for i in rng.choice(n, size=min(n, args.plain_subset), replace=False)]
+    plain = run_plain_subset(M, sub, D.local)
     return {"metric": "MCRG solves/s", "value": round(n / wall, 2), "unit": "solves/s", "n_gpus": D.world,
+            "plain": plain, "served_over_plain_solves": round((n / wall) / plain["solves_per_s"], 2),
             "steps": 1, "warmup": 0, "ms_per_step": round(wall * 1e3, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "p50_latency_s": round(float(np.percentile(lat, 50)), 4),

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <deque>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -301,8 +302,11 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
 struct mcrg_server {
   mcrg_server_cfg cfg;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_hbm;
   std::thread worker;
+  std::vector<std::thread> hbm_workers;  // run HBM-path requests concurrently
+  std::deque<void*> hbm_queue;           // admitted slots waiting for an HBM worker
+  bool hbm_stop = false;
   bool stop = false;
   uint64_t next_ticket = 1;
   struct Req {
@@ -374,6 +378,71 @@ struct Slot {
   bool tiled = false;
 };
 
+constexpr int kHbmWorkers = 4;
+
+// One HBM-path worker: takes admitted slots from the queue and runs them on
+// contexts it keeps per (L, levels, couplings), re-initialised per request so
+// that no request pays a device allocation (which can synchronise the device
+// and stall the other slots).
+void hbm_worker(mcrg_server* s) {
+  cudaSetDevice(s->cfg.device);
+  std::map<std::tuple<int, int, int>, mcrg_ctx*> cache;
+  for (;;) {
+    Slot* sl = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_hbm.wait(lk, [&] { return s->hbm_stop || !s->hbm_queue.empty(); });
+      if (s->hbm_queue.empty()) break;  // stop requested and nothing left
+      sl = static_cast<Slot*>(s->hbm_queue.front());
+      s->hbm_queue.pop_front();
+    }
+    mcrg_result res;
+    memset(&res, 0, sizeof res);
+    res.submit_s = sl->submit_s;
+    const mcrg_request& r = sl->r;
+    if (r.L > MCRG_SMEM_MAX_L && make_accept(r.K).fast) {
+      const auto key = std::make_tuple(r.L, sl->nl, r.n_couplings);
+      mcrg_ctx* c = nullptr;
+      int rc = MCRG_OK;
+      auto it = cache.find(key);
+      if (it != cache.end()) {
+        c = it->second;
+        rc = reinit_context(c, r.K, r.seed, r.replica);
+      } else {
+        mcrg_cfg cfg;
+        memset(&cfg, 0, sizeof cfg);
+        cfg.L = r.L;
+        cfg.b = 2;
+        cfg.n_levels = sl->nl;
+        cfg.n_couplings = r.n_couplings;
+        cfg.K = r.K;
+        cfg.seed = r.seed;
+        cfg.replica = r.replica;
+        cfg.device = s->cfg.device;
+        rc = mcrg_alloc(&c, &cfg);
+        if (!rc) cache[key] = c;
+      }
+      if (!rc) rc = mcrg_sweep(c, r.n_eq);
+      if (!rc) rc = mcrg_measure(c, r.n_samples, r.sweeps_between, &res.moments, 0, nullptr, 0);
+      res.status = rc;
+    } else {  // resident sizes outside the fast acceptance regime: a one-off context
+      res.status = run_tiled_request(&r, s->cfg.device, &res.moments);
+    }
+    res.done_s = mono_s();
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->done[sl->ticket] = res;
+    s->submitted.erase(sl->ticket);
+    arena_free(s, sl->off, sl->bytes);
+    s->bytes_in_use -= (int64_t)sl->bytes;
+    s->in_flight--;
+    s->completed++;
+    sl->busy = false;
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();
+  }
+  for (auto& kv : cache) mcrg_free(kv.second);
+}
+
 void server_loop(mcrg_server* s) {
   cudaSetDevice(s->cfg.device);
   std::vector<Slot> slots((size_t)s->cfg.slots);
@@ -418,7 +487,7 @@ void server_loop(mcrg_server* s) {
       sl.submit_s = q.submit_s;
       sl.nb = n_dev_bins(&q.r);
       sl.tiled = !(q.r.L <= MCRG_SMEM_MAX_L && make_accept(q.r.K).fast);
-      if (sl.tiled) continue;  // run synchronously below
+      if (sl.tiled) continue;  // handed to the HBM workers below
       uint8_t* base = s->arena + sl.off;
       ChainJob* d_job = reinterpret_cast<ChainJob*>(base);
       mcrg_moments* d_bins = reinterpret_cast<mcrg_moments*>(base + 256);
@@ -437,29 +506,21 @@ void server_loop(mcrg_server* s) {
         cudaMemcpyAsync(sl.h_bins, d_bins, sizeof(mcrg_moments) * (size_t)sl.nb, cudaMemcpyDeviceToHost, sl.stream);
       cudaEventRecord(sl.done, sl.stream);
     }
-    // ---- run tiled admissions (HBM path, synchronous on this thread)
-    for (auto& lp : launch) {
-      Slot& sl = *lp.first;
-      if (!sl.tiled) continue;
-      mcrg_result res;
-      memset(&res, 0, sizeof res);
-      res.submit_s = sl.submit_s;
-      res.status = run_tiled_request(&sl.r, s->cfg.device, &res.moments);
-      res.done_s = mono_s();
+    // ---- hand HBM-path admissions to the worker pool (they run concurrently, each on its own stream)
+    {
+      bool any = false;
       std::lock_guard<std::mutex> lk(s->mu);
-      s->done[sl.ticket] = res;
-      s->submitted.erase(sl.ticket);
-      arena_free(s, sl.off, sl.bytes);
-      s->bytes_in_use -= (int64_t)sl.bytes;
-      s->in_flight--;
-      s->completed++;
-      sl.busy = false;
-      s->cv_done.notify_all();
+      for (auto& lp : launch)
+        if (lp.first->tiled) {
+          s->hbm_queue.push_back(lp.first);
+          any = true;
+        }
+      if (any) s->cv_hbm.notify_all();
     }
     // ---- retire finished slots
     bool progressed = false;
     for (auto& sl : slots) {
-      if (!sl.busy || sl.tiled) continue;
+      if (sl.tiled || !sl.busy) continue;  // HBM-path slots are retired by their worker
       const cudaError_t q = cudaEventQuery(sl.done);
       if (q == cudaErrorNotReady) continue;
       mcrg_result res;
@@ -510,6 +571,7 @@ int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg) {
   }
   s->free_list[0] = (size_t)s->budget & ~size_t(255);
   s->worker = std::thread(server_loop, s);
+  for (int w = 0; w < kHbmWorkers; ++w) s->hbm_workers.emplace_back(hbm_worker, s);
   *out = s;
   return MCRG_OK;
 }
@@ -597,7 +659,14 @@ int mcrg_server_destroy(mcrg_server* s) {
     s->cv_work.notify_all();
     s->cv_done.notify_all();
   }
-  if (s->worker.joinable()) s->worker.join();
+  if (s->worker.joinable()) s->worker.join();  // returns once every admitted request is done
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->hbm_stop = true;
+    s->cv_hbm.notify_all();
+  }
+  for (auto& t : s->hbm_workers)
+    if (t.joinable()) t.join();
   cudaSetDevice(s->cfg.device);
   cudaFree(s->arena);
   delete s;

@@ -582,3 +582,25 @@ int mcrg_rgnn_scalar_output(mcrg_ctx* c, const double* W, double* out) {
   CK(cudaStreamSynchronize(c->stream));
   return MCRG_OK;
 }
+
+namespace mcrg {
+
+// Starts a new chain on an HBM-resident context (same L, levels, couplings
+// and device) without allocating: new K, seed and replica, fresh initial
+// coin, counters at zero.  Used by the server's workers to reuse contexts.
+int reinit_context(mcrg_ctx* c, double K, uint64_t seed, uint32_t replica) {
+  if (!c || !c->is_tiled || !std::isfinite(K)) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const Accept acc = make_accept(K);
+  const int rc = tiled_reinit(&c->tiled, Key{(uint32_t)seed, (uint32_t)(seed >> 32)}, replica, acc, c->stream);
+  if (rc) return rc;
+  c->cfg.K = K;
+  c->cfg.seed = seed;
+  c->cfg.replica = replica;
+  c->acc = acc;
+  c->t = 0;
+  c->n = 0;
+  return MCRG_OK;
+}
+
+}  // namespace mcrg

@@ -125,9 +125,15 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
     for (int l = 0; l <= nl; ++l, m >>= 1) {
       const uint8_t* lev = smem + plan.off[l];
       int a5[5] = {0, 0, 0, 0, 0};
-      if (m >= 32) couplings_vec<4>(lev, m, tid, T, a5);
-      else if (m == 16) couplings_vec<2>(lev, m, tid, T, a5);
-      else couplings_scalar(lev, m, tid, T, a5);
+      if (m >= 32) {
+        if (C <= 2) couplings_vec<4, 2>(lev, m, tid, T, a5);
+        else couplings_vec<4>(lev, m, tid, T, a5);
+      } else if (m == 16) {
+        if (C <= 2) couplings_vec<2, 2>(lev, m, tid, T, a5);
+        else couplings_vec<2>(lev, m, tid, T, a5);
+      } else {
+        couplings_scalar(lev, m, tid, T, a5);
+      }
       reduce_into(a5, S + l * MCRG_MAX_COUPLINGS, C);
       if (l < nl) {
         uint8_t* nxt = smem + plan.off[l + 1];

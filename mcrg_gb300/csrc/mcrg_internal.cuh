@@ -86,6 +86,9 @@ cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const 
                               Key key, uint32_t replica, int level, uint32_t sample, cudaStream_t s);
 cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out, cudaStream_t s);
 
+// New chain on an HBM-resident context without allocating (mcrg_capi.cu).
+int reinit_context(mcrg_ctx* c, double K, uint64_t seed, uint32_t replica);
+
 // Forward pass of the RG neural network (src/rgnn.cpp:281-307) on a split
 // layout lattice of side n: the scalar output into *d_out (device), using
 // `work` ((n/32)^2 + (n/1024)^2 + 2 doubles, not overlapping d_out).

@@ -266,7 +266,8 @@ __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key 
 // directional sums (each symmetric pair counted twice, as src/lattice.cpp
 // counts every bond from both ends).  Accumulates final values in acc[5].
 // ---------------------------------------------------------------------------
-template <int NW>
+// NC: number of couplings wanted (1..5); the sums past NC stay 0.
+template <int NW, int NC = 5>
 __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&acc)[5]) {
   constexpr int CB = 4 * NW;
   const int half = n / 2, cpr = half / CB;
@@ -283,14 +284,14 @@ __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&a
     const uint8_t* Od3 = O + (size_t)((i + 3) & (n - 1)) * half;
     uint32_t ci[NW], cd[NW], cd2[NW], oi[NW], od[NW], od3[NW];
     load_words<NW>(Ci + k0, ci);
-    load_words<NW>(Cd + k0, cd);
-    load_words<NW>(Cd2 + k0, cd2);
     load_words<NW>(Oi + k0, oi);
     load_words<NW>(Od + k0, od);
-    load_words<NW>(Od3 + k0, od3);
+    if (NC > 1) load_words<NW>(Cd + k0, cd);
+    if (NC > 2) load_words<NW>(Cd2 + k0, cd2);
+    if (NC > 4) load_words<NW>(Od3 + k0, od3);
     const int kn = (k0 + CB) & (half - 1), kp = (k0 - 4) & (half - 1);
-    const uint32_t ci_n = load_word(Ci + kn), oi_n = load_word(Oi + kn);
-    const uint32_t cd_n = load_word(Cd + kn), cd_p = load_word(Cd + kp);
+    const uint32_t ci_n = NC > 2 ? load_word(Ci + kn) : 0u, oi_n = load_word(Oi + kn);
+    const uint32_t cd_n = NC > 1 ? load_word(Cd + kn) : 0u, cd_p = NC > 1 ? load_word(Cd + kp) : 0u;
     uint32_t a = 0, b = 0, e = 0, p = 0, h = 0;
 #pragma unroll
     for (int j = 0; j < NW; ++j) {
@@ -305,16 +306,16 @@ __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&a
       const uint32_t cdqm = __funnelshift_rc(cd_pv, cd[j], 24 + 8 * q);  // C[i+1][k+q-1]
       const uint32_t x = ci[j];
       a += (x ^ od[j]) + (x ^ oiq);
-      b += (x ^ cdq) + (x ^ cdqm);
-      e += (x ^ cd2[j]) + (x ^ ci1);
-      p += x ^ od[j] ^ oiq ^ cdq;
-      h += (x ^ oiq ^ ci1 ^ oiq1) + (x ^ od[j] ^ cd2[j] ^ od3[j]);
+      if (NC > 1) b += (x ^ cdq) + (x ^ cdqm);
+      if (NC > 2) e += (x ^ cd2[j]) + (x ^ ci1);
+      if (NC > 3) p += x ^ od[j] ^ oiq ^ cdq;
+      if (NC > 4) h += (x ^ oiq ^ ci1 ^ oiq1) + (x ^ od[j] ^ cd2[j] ^ od3[j]);
     }
     acc[0] += 4 * CB - 4 * (int)bytesum(a);
-    acc[1] += 4 * CB - 4 * (int)bytesum(b);
-    acc[2] += 4 * CB - 4 * (int)bytesum(e);
-    acc[3] += CB - 2 * (int)bytesum(p);
-    acc[4] += 2 * CB - 2 * (int)bytesum(h);
+    if (NC > 1) acc[1] += 4 * CB - 4 * (int)bytesum(b);
+    if (NC > 2) acc[2] += 4 * CB - 4 * (int)bytesum(e);
+    if (NC > 3) acc[3] += CB - 2 * (int)bytesum(p);
+    if (NC > 4) acc[4] += 2 * CB - 2 * (int)bytesum(h);
   }
 }
 

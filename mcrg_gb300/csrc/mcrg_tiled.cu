@@ -240,6 +240,18 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
 }
 
+int tiled_reinit(TiledLattice* t, Key key, uint32_t replica, const Accept& acc, cudaStream_t s) {
+  if (!acc.fast) return MCRG_ENOSYS;
+  t->key = key;
+  t->replica = replica;
+  t->acc = acc;
+  cudaMemsetAsync(t->d_S, 0, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS, s);
+  cudaMemsetAsync(t->d_status, 0, sizeof(int), s);
+  tiled_init_kernel<<<g_num_sms * 8, 256, 0, s>>>(t->buf[0], t->L, key, replica);
+  t->cur = 0;
+  return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
+}
+
 void tiled_free(TiledLattice* t) {
   cudaFree(t->buf[0]);
   cudaFree(t->buf[1]);

@@ -24,6 +24,9 @@ struct TiledLattice {
 int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica, const Accept& acc,
                 cudaStream_t s);
 void tiled_free(TiledLattice* t);
+// New chain on an allocated lattice: new key, replica and acceptance, fresh
+// initial coin, the autotuned sweep variant kept (no allocation).
+int tiled_reinit(TiledLattice* t, Key key, uint32_t replica, const Accept& acc, cudaStream_t s);
 uint8_t* tiled_state(TiledLattice* t);
 // n sweeps starting at sweep index t0 (one fused two-colour pass per sweep).
 int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s);

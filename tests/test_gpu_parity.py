@@ -246,6 +246,32 @@ def test_server_alone_and_in_the_mix(M):
         srv.close()
 
 
+def test_server_hbm_requests_in_the_mix(M):
+    """HBM-size requests (L > 256) run on the server's worker pool, several with the same L
+    so that cached contexts are re-initialised between requests; every result equals the
+    single-context run of the same request, alone and while small requests run."""
+    rng = np.random.default_rng(5)
+    reqs = []
+    for i in range(14):
+        L = int(rng.choice([512, 1024])) if i % 2 == 0 else int(rng.choice([16, 64, 256]))
+        reqs.append(M.make_request(L, float(rng.uniform(-0.49, -0.43)), seed=300 + i, replica=i,
+                                   n_eq=int(rng.integers(0, 4)), n_samples=int(rng.integers(1, 4)),
+                                   sweeps_between=int(rng.integers(1, 3)), n_couplings=int(rng.choice([2, 5]))))
+    srv = M.Server(slots=6, hbm_budget_bytes=1 << 30)
+    try:
+        tickets = [srv.submit(r) for r in reqs]
+        out = [srv.wait(t, 300) for t in tickets]
+        for r, o in zip(reqs, out):
+            assert o.status == 0, (r.L, o.status)
+            assert_moments_equal(M.moments_from_c(o.moments), solo(M, r))
+        again = srv.wait(srv.submit(reqs[0]), 300)  # a reused context gives the same chain again
+        assert_moments_equal(M.moments_from_c(again.moments), M.moments_from_c(out[0].moments))
+        st = srv.stats()
+        assert st["completed"] == len(reqs) + 1 and st["in_flight"] == 0 and st["bytes_in_use"] == 0
+    finally:
+        srv.close()
+
+
 def test_server_admission_errors(M):
     from mcrg_gb300 import _abi
     srv = M.Server(slots=1, hbm_budget_bytes=1 << 20, queue_capacity=1)
