@@ -378,7 +378,7 @@ struct Slot {
   bool tiled = false;
 };
 
-constexpr int kHbmWorkers = 4;
+constexpr int kHbmWorkers = 16;  // HBM-path requests are small, latency-bound launches: overlap many
 
 // One HBM-path worker: takes admitted slots from the queue and runs them on
 // contexts it keeps per (L, levels, couplings), re-initialised per request so

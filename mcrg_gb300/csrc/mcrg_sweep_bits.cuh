@@ -220,14 +220,19 @@ __device__ __forceinline__ void resolve_queue(int c, int g, int first, int strid
 // issues the bulk copies.  (A dedicated helper warp for the copies and the
 // open sites, and drawing the Philox blocks ahead of the copy wait, both
 // measured slower on GB300.)
-template <int NT, int MINB, int LEAD, int LW>
+// WPT plane words per thread per colour and group: a group is NS = NT * WPT
+// words; slot s = tid + j NT (j < WPT) of a thread is row s / WPR, word s % WPR
+// of the group, so that a thread's words are independent chains (ILP) and the
+// per-phase fixed work is shared by more sites.
+template <int NT, int WPT, int MINB, int LEAD, int LW>
 __global__ void __launch_bounds__(NT, MINB)
     sweep_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const __grid_constant__ Params P,
                  uint32_t tt, int* __restrict__ status) {
-  using G = Geo<NT, LW, LEAD>;
+  constexpr int NS = NT * WPT;
+  using G = Geo<NS, LW, LEAD>;
   constexpr int L = G::L, H = G::H, WPR = G::WPR, R = G::R, RAW_ROWS = G::RAW_ROWS, PK_ROWS = G::PK_ROWS;
   constexpr size_t PLANE = G::PLANE;
-  constexpr int kRawSlots = LEAD + 1, CAP = queue_cap<NT>();
+  constexpr int kRawSlots = LEAD + 1, CAP = queue_cap<NS>();
   extern __shared__ __align__(128) uint8_t smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   int* qn = reinterpret_cast<int*>(smem + 64);                    // [colour][3] queue lengths
@@ -236,8 +241,13 @@ __global__ void __launch_bounds__(NT, MINB)
   uint32_t* pk = reinterpret_cast<uint32_t*>(raw + 2 * (size_t)RAW_ROWS * H);  // [colour][PK_ROWS][WPR]
   uint32_t* pk1 = pk + PK_ROWS * WPR;
 
-  const int tid = threadIdx.x, w = tid % WPR, lane = tid & 31;
-  const int rr = (R == 1) ? 0 : tid / WPR;  // row within a group (uniform when groups are one row)
+  const int tid = threadIdx.x, lane = tid & 31;
+  int wj[WPT], rj[WPT];  // word and row (within the group) of each slot of this thread
+#pragma unroll
+  for (int j = 0; j < WPT; ++j) {
+    wj[j] = (tid + j * NT) % WPR;
+    rj[j] = (R == 1) ? 0 : (tid + j * NT) / WPR;  // uniform when groups are one row
+  }
   const int b0 = (int)(((long long)blockIdx.x * L) / gridDim.x);
   const int b1 = (int)(((long long)(blockIdx.x + 1) * L) / gridDim.x);
   const int top = b0 - 2;
@@ -249,7 +259,7 @@ __global__ void __launch_bounds__(NT, MINB)
   if (tid == 0) tma::fence_mbar_init();
   __syncthreads();
   if (tid < 32)
-    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NT, LW, LEAD>(g, top, b0, b1, ms, in, raw, bar, lane);
+    for (int g = 0; g < LEAD && g < J; ++g) issue_group<NS, LW, LEAD>(g, top, b0, b1, ms, in, raw, bar, lane);
 
   // ok turns false when a bulk copy does not land in time; the phase's work
   // then runs on stale shared memory (all indices stay in bounds) and the
@@ -269,27 +279,31 @@ __global__ void __launch_bounds__(NT, MINB)
     {
       const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
       if (STEADY || (g >= 0 && g < J))
-        resolve_queue<NT, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
+        resolve_queue<NS, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
     }
     // ---- bulk copies of group p + LEAD (its slot was packed last phase)
-    if (tid < 32 && p + LEAD < J) issue_group<NT, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
+    if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
     // ---- pack group p
     if (STEADY || p < J) {
       if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
-      const int off = p * R + rr, x = top + off;
-      const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
-      if (STEADY || (x >= b0 - 1 && x <= b1)) {
-        const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
-        pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
-      }
-      if (STEADY || x <= b1 + 1) {
-        const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
-        pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+#pragma unroll
+      for (int j = 0; j < WPT; ++j) {
+        const int w = wj[j], off = p * R + rj[j], x = top + off;
+        const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
+        if (STEADY || (x >= b0 - 1 && x <= b1)) {
+          const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
+          pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+        }
+        if (STEADY || x <= b1 + 1) {
+          const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
+          pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+        }
       }
     }
     // ---- colour 0 of group p-2
-    {
-      const int off = (p - 2) * R + rr, x = top + off;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      const int w = wj[j], off = (p - 2) * R + rj[j], x = top + off;
       if (STEADY || (p >= 2 && p - 2 < J && x >= b0 - 1 && x <= b1)) {
         const int gr = lattice_row(x, ms, L), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk[pi * WPR + w];
@@ -303,13 +317,14 @@ __global__ void __launch_bounds__(NT, MINB)
         const uint4 B = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue<NT>(open, zero, t, off, w, gr, 0, (p - 2) % 3, qn, Q, P, tt);
+        if (open) nt ^= enqueue<NS>(open, zero, t, off, w, gr, 0, (p - 2) % 3, qn, Q, P, tt);
         pk[pi * WPR + w] = nt;
       }
     }
     // ---- colour 1 of group p-5, then both colours of its rows to the output
-    {
-      const int off = (p - 5) * R + rr, x = top + off;
+#pragma unroll
+    for (int j = 0; j < WPT; ++j) {
+      const int w = wj[j], off = (p - 5) * R + rj[j], x = top + off;
       if (STEADY || (p >= 5 && p - 5 < J && x >= b0 && x <= b1 - 1)) {
         const int gr = lattice_row(x, ms, L), pi = off & (PK_ROWS - 1);
         const uint32_t t = pk1[pi * WPR + w];
@@ -323,7 +338,7 @@ __global__ void __launch_bounds__(NT, MINB)
         const uint4 B = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue<NT>(open, zero, t, off, w, gr, 1, 3 + (p - 5) % 3, qn, Q, P, tt);
+        if (open) nt ^= enqueue<NS>(open, zero, t, off, w, gr, 1, 3 + (p - 5) % 3, qn, Q, P, tt);
         uint4 a, b;
         unpack_bytes(mid, a, b);
         uint4* o0 = reinterpret_cast<uint4*>(out + (size_t)gr * H + 32 * w);

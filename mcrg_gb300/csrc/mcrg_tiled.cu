@@ -147,32 +147,38 @@ int g_num_sms = 0;
 // eligible variant on the live lattice.
 struct Variant {
   int threads, lw, lead;  // threads per CTA, L = 64 << lw, row groups in flight ahead of packing
+  int wpt;                // plane words per thread per colour and group
   const void* kern;
   size_t smem;
   int waves;              // bands = waves x resident CTAs (two waves measured slower: more halo rows)
 };
 
-#define BITS_VARIANT_W(NT_, MINB_, LEAD_, LW_, W_)                                                      \
+#define BITS_VARIANT_X(NT_, WPT_, MINB_, LEAD_, LW_)                                                    \
   Variant {                                                                                              \
-    NT_, LW_, LEAD_, (const void*)bits::sweep_kernel<NT_, MINB_, LEAD_, LW_>, bits::smem_bytes<NT_, LEAD_>(), W_ \
+    NT_, LW_, LEAD_, WPT_, (const void*)bits::sweep_kernel<NT_, WPT_, MINB_, LEAD_, LW_>,               \
+        bits::smem_bytes<NT_ * WPT_, LEAD_>(), 1                                                         \
   }
-#define BITS_VARIANT(NT_, MINB_, LEAD_, LW_) BITS_VARIANT_W(NT_, MINB_, LEAD_, LW_, 1)
-// per side: 256 threads x 3 CTAs per SM (copy lead 2), x 4 (lead 1), x 2 (lead 3), 512 x 1, 128 x 4
+#define BITS_VARIANT(NT_, MINB_, LEAD_, LW_) BITS_VARIANT_X(NT_, 1, MINB_, LEAD_, LW_)
+// per side: 256 threads x 3 CTAs per SM (copy lead 2), x 4 (lead 1), x 2 (lead 3), 512 x 1, 128 x 4;
+// and 128 threads with two words each (x 4 CTAs per SM, lead 1 or 2)
 #define BITS_VARIANTS_L(LW_)                                                                             \
   BITS_VARIANT(256, 3, 2, LW_), BITS_VARIANT(256, 4, 1, LW_), BITS_VARIANT(256, 2, 3, LW_),             \
-      BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_)
+      BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_), BITS_VARIANT_X(128, 2, 4, 1, LW_)
 
-const Variant kVariants[] = {BITS_VARIANT(256, 4, 1, 8), BITS_VARIANT(256, 3, 2, 8), BITS_VARIANT(256, 2, 3, 8),
-                             BITS_VARIANT(512, 1, 3, 8), BITS_VARIANTS_L(7),          BITS_VARIANTS_L(6),
-                             BITS_VARIANTS_L(5),          BITS_VARIANTS_L(4),          BITS_VARIANTS_L(3)};
+const Variant kVariants[] = {BITS_VARIANT(256, 4, 1, 8),        BITS_VARIANT(256, 3, 2, 8),
+                             BITS_VARIANT(256, 2, 3, 8),        BITS_VARIANT(512, 1, 3, 8),
+                             BITS_VARIANT_X(128, 2, 4, 1, 8),    BITS_VARIANT_X(128, 2, 4, 2, 8),
+                             BITS_VARIANT_X(256, 2, 2, 1, 8),    BITS_VARIANTS_L(7),
+                             BITS_VARIANTS_L(6),                 BITS_VARIANTS_L(5),
+                             BITS_VARIANTS_L(4),                 BITS_VARIANTS_L(3)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int block_threads(const Variant& v) { return v.threads; }
 
-bool variant_fits(const Variant& v, int L) { return (64 << v.lw) == L; }
+bool variant_fits(const Variant& v, int L) { return (64 << v.lw) == L && (v.threads * v.wpt) >= (L / 64); }
 
 // rows per pipeline group
-int variant_rows(const Variant& v) { return v.threads >> v.lw; }
+int variant_rows(const Variant& v) { return (v.threads * v.wpt) >> v.lw; }
 
 void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* out, uint32_t tt, cudaStream_t s) {
   const Variant& v = kVariants[vi];
@@ -273,11 +279,11 @@ static int autotune(TiledLattice* t, cudaStream_t s) {
   static std::map<std::pair<int, int>, int> cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>l<lead>[w<waves>]" forces a variant
-    int nt = 0, lead = 2, waves = 1;
-    if (force[0] == 'b' && sscanf(force + 1, "%dl%dw%d", &nt, &lead, &waves) >= 1)
+  if (const char* force = getenv("MCRG_TILE")) {  // "b<threads>l<lead>[x<words per thread>]" forces a variant
+    int nt = 0, lead = 2, wpt = 1;
+    if (force[0] == 'b' && sscanf(force + 1, "%dl%dx%d", &nt, &lead, &wpt) >= 1)
       for (int v = 0; v < kNumVariants; ++v)
-        if (kVariants[v].threads == nt && kVariants[v].lead == lead && kVariants[v].waves == waves &&
+        if (kVariants[v].threads == nt && kVariants[v].lead == lead && kVariants[v].wpt == wpt &&
             variant_fits(kVariants[v], t->L))
           return v;
   }

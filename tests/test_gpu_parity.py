@@ -334,7 +334,7 @@ def test_device_chain_matches_reference_L8(M, golden):
 # every sweep variant of the HBM path (bit-sliced band streaming, threads per CTA)
 # --------------------------------------------------------------------------
 def _variants_for(N):
-    out = ["b256l2", "b256l1", "b256l3", "b512l3"]
+    out = ["b256l2", "b256l1", "b256l3", "b512l3", "b128l1x2"]
     if N // 64 <= 128:
         out.append("b128l3")
     return out
@@ -350,7 +350,8 @@ def test_every_sweep_variant_bit_exact(M, N, monkeypatch):
         lat.sweep(2)
         got = lat.spins_
         rows, threads = lat.tile_shape()
-        assert threads == int(v[1:].split("l")[0]) and rows * (N // 64) == threads
+        wpt = int(v.split("x")[1]) if "x" in v else 1
+        assert threads == int(v[1:].split("l")[0]) and rows * (N // 64) == threads * wpt
         lat.close()
         np.testing.assert_array_equal(got, ref, err_msg="variant %s" % v)
 
@@ -362,7 +363,7 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
     init = O.init_spins(N, 5, 0)
     ref = O.sweep(init, KC, 5, 0, 0, 1)
     ref_S = O.couplings(ref, 5)
-    for v in ("b256l2", "b256l1", "b512l3"):
+    for v in ("b256l2", "b256l1", "b512l3", "b128l1x2", "b128l2x2", "b256l1x2"):
         monkeypatch.setenv("MCRG_TILE", v)
         lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
         lat.sweep(1)
