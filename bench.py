@@ -362,7 +362,8 @@ def run_served(args, D: Dist) -> dict:
 
     rates = {}
     all_reqs = []
-    srv = M.Server(device=D.local, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)))
+    srv = M.Server(device=D.local, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)),
+                   hbm_workers=args.served_hbm_workers)
     try:
         for rate in (1e2, 1e3, 1e4):
             n = int(min(args.served_requests, max(50, 2 * rate)))
@@ -500,6 +501,7 @@ def main():
     ap.add_argument("--served-scale", type=float, default=0.01)
     ap.add_argument("--served-slots", type=int, default=512)
     ap.add_argument("--served-budget-gb", type=float, default=150.0)
+    ap.add_argument("--served-hbm-workers", type=int, default=0, help="host threads for L > 256 requests (0: 16)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

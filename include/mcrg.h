@@ -261,7 +261,8 @@ typedef struct {
   int32_t slots;            /* concurrent resident chains (CTAs) */
   int64_t hbm_budget_bytes; /* device bytes the server may hold for lattices */
   int32_t queue_capacity;   /* pending requests before mcrg_submit returns EBUSY */
-  int32_t pad;
+  int32_t hbm_workers;      /* host threads running HBM-size requests (L > MCRG_SMEM_MAX_L) concurrently;
+                               0 selects 16, at most 256 */
 } mcrg_server_cfg;
 
 typedef struct mcrg_server mcrg_server;

@@ -289,8 +289,9 @@ def batch_run(requests, device: int = 0, use_graph: bool = True, raw: bool = Fal
 class Server:
     """Continuous-batching MCRG server (mcrg_server_*)."""
 
-    def __init__(self, device: int = 0, slots: int = 256, hbm_budget_bytes: int = 1 << 30, queue_capacity: int = 1 << 16):
-        cfg = _abi.ServerCfg(device, slots, hbm_budget_bytes, queue_capacity, 0)
+    def __init__(self, device: int = 0, slots: int = 256, hbm_budget_bytes: int = 1 << 30, queue_capacity: int = 1 << 16,
+                 hbm_workers: int = 0):
+        cfg = _abi.ServerCfg(device, slots, hbm_budget_bytes, queue_capacity, hbm_workers)
         h = C.c_void_p()
         check(lib().mcrg_server_create(C.byref(h), C.byref(cfg)), "mcrg_server_create")
         self._h = h

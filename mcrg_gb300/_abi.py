@@ -65,7 +65,7 @@ class Result(C.Structure):
 
 class ServerCfg(C.Structure):
     _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("hbm_budget_bytes", C.c_int64),
-                ("queue_capacity", C.c_int32), ("pad", C.c_int32)]
+                ("queue_capacity", C.c_int32), ("hbm_workers", C.c_int32)]
 
 
 P = C.POINTER

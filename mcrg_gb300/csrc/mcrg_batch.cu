@@ -378,7 +378,8 @@ struct Slot {
   bool tiled = false;
 };
 
-constexpr int kHbmWorkers = 16;  // HBM-path requests are small, latency-bound launches: overlap many
+constexpr int kHbmWorkersDefault = 16;  // HBM-path requests are small, latency-bound launches: overlap many
+constexpr int kHbmWorkersMax = 256;
 
 // One HBM-path worker: takes admitted slots from the queue and runs them on
 // contexts it keeps per (L, levels, couplings), re-initialised per request so
@@ -557,7 +558,8 @@ void server_loop(mcrg_server* s) {
 extern "C" {
 
 int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg) {
-  if (!out || !cfg || cfg->slots < 1 || cfg->slots > 4096 || cfg->hbm_budget_bytes <= 0 || cfg->queue_capacity < 1)
+  if (!out || !cfg || cfg->slots < 1 || cfg->slots > 4096 || cfg->hbm_budget_bytes <= 0 || cfg->queue_capacity < 1 ||
+      cfg->hbm_workers < 0 || cfg->hbm_workers > kHbmWorkersMax)
     return MCRG_EINVAL;
   *out = nullptr;
   if (cudaSetDevice(cfg->device) != cudaSuccess) return MCRG_EIO;
@@ -571,7 +573,8 @@ int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg) {
   }
   s->free_list[0] = (size_t)s->budget & ~size_t(255);
   s->worker = std::thread(server_loop, s);
-  for (int w = 0; w < kHbmWorkers; ++w) s->hbm_workers.emplace_back(hbm_worker, s);
+  const int nw = cfg->hbm_workers > 0 ? cfg->hbm_workers : kHbmWorkersDefault;
+  for (int w = 0; w < nw; ++w) s->hbm_workers.emplace_back(hbm_worker, s);
   *out = s;
   return MCRG_OK;
 }
