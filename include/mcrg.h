@@ -62,6 +62,8 @@ extern "C" {
 #define MCRG_MAX_COUPLINGS 5
 #define MCRG_MAX_L 16384
 #define MCRG_SMEM_MAX_L 256    /* lattices up to this side run shared-memory resident */
+#define MCRG_RESIDENT_MAX_L 1024 /* batched / served chains in the fast acceptance regime run
+                                    shared-memory resident up to this side (bit-plane levels) */
 
 enum {
   MCRG_OK = 0,

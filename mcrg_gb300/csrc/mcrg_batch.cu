@@ -1,10 +1,11 @@
 // mcrg_batch.cu -- batched and served MCRG solves.
 //
-// Batched (mcrg_batch_run): every request of side <= MCRG_SMEM_MAX_L becomes
-// one shared-memory-resident chain (one CTA); all chains of one side run in
-// one launch and the launches of different sides run concurrently on fork /
-// join streams, captured into a CUDA graph when asked.  Larger sides run on
-// the HBM-tiled path afterwards.  This replaces the reference's one chain per
+// Batched (mcrg_batch_run): every request in the fast acceptance regime of
+// side <= MCRG_RESIDENT_MAX_L becomes one shared-memory-resident chain (one
+// CTA; levels of side >= 64 as bit planes); all chains of one side run in one
+// launch and the launches of different sides run concurrently on fork / join
+// streams, captured into a CUDA graph when asked.  Larger sides and the other
+// acceptance regimes run on the per-lattice path afterwards.  This replaces the reference's one chain per
 // MPI rank + MPI_Allreduce (src/mcrg.cpp:42,101-103).
 //
 // Served (mcrg_server_*): a scheduler thread admits queued requests as slots
@@ -212,7 +213,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
   std::vector<int64_t> bin_off(n, 0);
   for (int i = 0; i < n; ++i) {
     if (results[i].status) continue;
-    if (reqs[i].L <= MCRG_SMEM_MAX_L && make_accept(reqs[i].K).fast) {
+    if (reqs[i].L <= MCRG_RESIDENT_MAX_L && make_accept(reqs[i].K).fast) {
       groups[reqs[i].L].push_back(i);
       state_off[i] = state_bytes;
       state_bytes += (size_t)reqs[i].L * reqs[i].L;
@@ -257,7 +258,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         int maxlev = 0;
         for (int q = 0; q < ranges[g].second; ++q) maxlev = std::max(maxlev, w.h_jobs[(size_t)ranges[g].first + q].n_levels);
         if (launch_chain(w.d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads,
-                         sg) != cudaSuccess)
+                         j0.L >= 64, sg) != cudaSuccess)  // every job of a group is in the fast regime
           rc = MCRG_EIO;
         cudaEventRecord(w.ev[g % kMaxGroups], sg);
         cudaStreamWaitEvent(s0, w.ev[g % kMaxGroups], 0);
@@ -426,7 +427,7 @@ void hbm_worker(mcrg_server* s) {
       if (!rc) rc = mcrg_sweep(c, r.n_eq);
       if (!rc) rc = mcrg_measure(c, r.n_samples, r.sweeps_between, &res.moments, 0, nullptr, 0);
       res.status = rc;
-    } else {  // resident sizes outside the fast acceptance regime: a one-off context
+    } else {  // outside the fast acceptance regime: a one-off context
       res.status = run_tiled_request(&r, s->cfg.device, &res.moments);
     }
     res.done_s = mono_s();
@@ -487,7 +488,7 @@ void server_loop(mcrg_server* s) {
       sl.nl = q.nl;
       sl.submit_s = q.submit_s;
       sl.nb = n_dev_bins(&q.r);
-      sl.tiled = !(q.r.L <= MCRG_SMEM_MAX_L && make_accept(q.r.K).fast);
+      sl.tiled = !(q.r.L <= MCRG_RESIDENT_MAX_L && make_accept(q.r.K).fast);
       if (sl.tiled) continue;  // handed to the HBM workers below
       uint8_t* base = s->arena + sl.off;
       ChainJob* d_job = reinterpret_cast<ChainJob*>(base);
@@ -502,7 +503,7 @@ void server_loop(mcrg_server* s) {
       }
       cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, sl.stream);
       cudaMemsetAsync(d_bins, 0, sizeof(mcrg_moments) * (size_t)(sl.nb > 0 ? sl.nb : 1), sl.stream);
-      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, sl.stream);
+      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, j.L >= 64, sl.stream);  // fast regime
       if (sl.nb > 0)
         cudaMemcpyAsync(sl.h_bins, d_bins, sizeof(mcrg_moments) * (size_t)sl.nb, cudaMemcpyDeviceToHost, sl.stream);
       cudaEventRecord(sl.done, sl.stream);

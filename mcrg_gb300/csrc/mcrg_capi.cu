@@ -160,7 +160,7 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   }
   j.bins = c->d_bins;
   CK(cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream));
-  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.C, j.threads, c->stream));
+  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.C, j.threads, j.acc.fast && j.L >= 64, c->stream));
   c->t += (uint64_t)(n_eq + n_samples * sweeps_between);
   c->n += (uint64_t)n_samples;
   *n_bins_out = nb;
@@ -254,7 +254,10 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
       j.key = key; j.replica = cfg->replica; j.init = 1; j.store = 1; j.bin_size = 1;
       j.state = c->d_state; j.acc = c->acc;
       if (cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
-      if (launch_chain(c->d_job, 1, j.L, nl, j.C, j.threads, c->stream) != cudaSuccess) { rc = MCRG_EIO; break; }
+      if (launch_chain(c->d_job, 1, j.L, nl, j.C, j.threads, j.acc.fast && j.L >= 64, c->stream) != cudaSuccess) {
+        rc = MCRG_EIO;
+        break;
+      }
     } else {
       c->is_tiled = true;
       rc = tiled_alloc(&c->tiled, cfg->L, nl, cfg->n_couplings, key, cfg->replica, c->acc, c->stream);

@@ -1,4 +1,6 @@
-// mcrg_chain.cu -- shared-memory-resident MCRG chain (lattice side L <= 256).
+// mcrg_chain.cu -- shared-memory-resident MCRG chain (lattice side L <= 256;
+// up to 1024 in the fast acceptance regime, where levels of side >= 64 are
+// bit planes).
 //
 // One CTA owns one lattice for the whole launch: it draws (or loads) the
 // configuration into shared memory, runs n_eq thermalisation sweeps, then
@@ -9,8 +11,9 @@
 // between the initial load and the final store except the per-bin moment
 // flushes.
 //
-// Sweep (L >= 64): bit-sliced on a plane-word copy of level 0
-// (mcrg_resident_bits.cuh), the bytes refreshed before each measurement.
+// Fast acceptance regime, L >= 64: every level of side >= 64 is kept only as
+// bit-plane words; sweeps, coupling sums and blocking of those levels run
+// bit-sliced (mcrg_resident_bits.cuh), the smaller levels as bytes.
 // Sweep (L <= 32): the 16 sites of a 16-byte chunk of one colour row are updated with
 // byte-SWAR arithmetic from one Philox block (one 8-bit draw per site).  A
 // site whose 8-bit draw equals the top byte of its threshold is left open and
@@ -48,7 +51,9 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   const Key key = J.key;
   const uint32_t rep = J.replica;
   const Accept acc = J.acc;
-  const SmemPlan plan = make_plan(L, nl, C);
+  // L >= 64 in the fast regime: levels of side >= 64 are plane words
+  const bool bits = acc.fast && L >= 64;
+  const SmemPlan plan = make_plan(L, nl, C, bits);
   uint8_t* lat = smem;
   int* S = reinterpret_cast<int*>(smem + plan.s_off);
   int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
@@ -57,14 +62,15 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   const int E = J.flow ? 2 * (nl + 1) : plan.E;
   uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (threadIdx.x >> 5) * kOpenPerWarp;
   const bool vec = acc.fast && L >= 16;
-  // L >= 64 in the fast regime: sweeps run on a plane-word copy of level 0
-  const bool bits = acc.fast && L >= 64;
-  uint32_t* pl = bits ? reinterpret_cast<uint32_t*>(smem + plan.pl_off) : nullptr;
-  int* qn = bits ? reinterpret_cast<int*>(smem + plan.pl_off + 2 * (L * L / 64) * 4) : nullptr;
+  uint32_t* pl = bits ? reinterpret_cast<uint32_t*>(smem) : nullptr;
+  int* qn = bits ? reinterpret_cast<int*>(smem + plan.qn_off) : nullptr;
   uint4* oq = bits ? reinterpret_cast<uint4*>(smem + plan.q_off) : nullptr;
 
   // ---- configuration into shared memory
-  if (J.init) {
+  if (bits) {
+    if (J.init) resident::init_planes(pl, L, key, rep, tid, T);
+    else resident::pack_lattice(J.state, pl, L, tid, T);
+  } else if (J.init) {
     init_level0(lat, L, key, rep, tid, T);
   } else {
     const uint4* src = reinterpret_cast<const uint4*>(J.state);
@@ -98,10 +104,6 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
   }
   if (bits && tid < 2) qn[tid] = 0;
   __syncthreads();
-  if (bits) {
-    resident::pack_lattice(lat, pl, L, tid, T);
-    __syncthreads();
-  }
 
   uint32_t t = J.t0;
   for (int64_t s = 0; s < J.n_eq; ++s) {
@@ -113,10 +115,6 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
       if (bits) resident::sweep(pl, L, t++, key, rep, acc, tid, T, oq, qn);
       else chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
     }
-    if (bits) {  // the measurement reads the byte lattice
-      resident::unpack_lattice(pl, lat, L, tid, T);
-      __syncthreads();
-    }
     // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
@@ -125,7 +123,11 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
     for (int l = 0; l <= nl; ++l, m >>= 1) {
       const uint8_t* lev = smem + plan.off[l];
       int a5[5] = {0, 0, 0, 0, 0};
-      if (m >= 32) {
+      if (bits && m >= 64) {
+        const uint32_t* P = reinterpret_cast<const uint32_t*>(lev);
+        if (C <= 2) resident::couplings_planes<2>(P, m, tid, T, a5);
+        else resident::couplings_planes<5>(P, m, tid, T, a5);
+      } else if (m >= 32) {
         if (C <= 2) couplings_vec<4, 2>(lev, m, tid, T, a5);
         else couplings_vec<4>(lev, m, tid, T, a5);
       } else if (m == 16) {
@@ -137,7 +139,9 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
       reduce_into(a5, S + l * MCRG_MAX_COUPLINGS, C);
       if (l < nl) {
         uint8_t* nxt = smem + plan.off[l + 1];
-        if (m >= 32) block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
+        if (bits && m >= 64)
+          resident::block_planes(reinterpret_cast<const uint32_t*>(lev), m, nxt, key, rep, l + 1, sample, tid, T);
+        else if (m >= 32) block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
         else block_scalar(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
       }
       __syncthreads();
@@ -178,10 +182,8 @@ __global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__
 
   // ---- final configuration back to HBM
   if (bits) {
-    resident::unpack_lattice(pl, lat, L, tid, T);
-    __syncthreads();
-  }
-  if (J.store) {
+    if (J.store) resident::unpack_lattice(pl, J.state, L, tid, T);
+  } else if (J.store) {
     const uint4* src = reinterpret_cast<const uint4*>(lat);
     uint4* dst = reinterpret_cast<uint4*>(J.state);
     for (int v = tid; v < L * L / 16; v += T) dst[v] = src[v];
@@ -208,14 +210,16 @@ __global__ void couplings_once_kernel(const uint8_t* in, int N, int C, int* out)
   reduce_into(a5, out, C);
 }
 
-cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads,
+cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
                          cudaStream_t stream) {
-  const SmemPlan plan = make_plan(L, n_levels, C);
-  static int configured = 0;
-  if (plan.bytes > configured) {
-    cudaError_t e = cudaFuncSetAttribute(chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  const SmemPlan plan = make_plan(L, n_levels, C, planes);
+  constexpr int kMaxSmem = 227 * 1024;  // opt-in shared memory per CTA
+  if (plan.bytes > kMaxSmem) return cudaErrorInvalidValue;
+  static int configured = 0;  // per process: the attribute is per function, set once for the largest plan
+  if (plan.bytes > 48 * 1024 && configured < kMaxSmem) {
+    cudaError_t e = cudaFuncSetAttribute(chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
     if (e != cudaSuccess) return e;
-    configured = 200 * 1024;
+    configured = kMaxSmem;
   }
   chain_kernel<<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
   return cudaGetLastError();

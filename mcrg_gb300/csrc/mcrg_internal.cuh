@@ -27,7 +27,9 @@ struct ChainJob {
 };
 
 // Shared-memory plan of a resident lattice, its blocked levels and (when
-// C > 0) the moment accumulators of one chain.
+// C > 0) the moment accumulators of one chain.  planes: every level of side
+// >= 64 is kept as bit-plane words (m^2 / 8 bytes) instead of bytes, and the
+// open-word queue of the bit-sliced sweep is added (mcrg_resident_bits.cuh).
 struct SmemPlan {
   int off[MCRG_MAX_LEVELS + 2];
   int s_off;    // int32 S[(MCRG_MAX_LEVELS+1) * MCRG_MAX_COUPLINGS]
@@ -36,17 +38,23 @@ struct SmemPlan {
   int scr_off;  // uint32 open-site scratch: 64 per warp, up to 8 warps
   int E;        // moment entries of the T-matrix moments
   int Ecap;     // entries the table holds (also fits the 2 (n_levels + 1) flow moments)
-  int pl_off;   // L >= 64: plane words of level 0 (2 L^2 / 64 uint32), then qn[2] and the open-word queue
-  int q_off;    // uint4 queue entries (resident::queue_cap(L))
+  int qn_off;   // planes: int qn[2] (padded to 16 bytes)
+  int q_off;    // planes: uint4 queue entries (resident queue_cap(L))
   int bytes;
 };
 
-__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
+// Largest side of a resident chain: bytes up to MCRG_SMEM_MAX_L, bit planes
+// (fast acceptance regime) up to MCRG_RESIDENT_MAX_L.
+__host__ __device__ inline bool resident_fits(int L, bool fast) {
+  return L <= (fast ? MCRG_RESIDENT_MAX_L : MCRG_SMEM_MAX_L);
+}
+
+__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bool planes = false) {
   SmemPlan p;
   int off = 0, n = L;
   for (int l = 0; l <= n_levels; ++l, n >>= 1) {
     p.off[l] = off;
-    off += ((n * n + 15) / 16) * 16;
+    off += (planes && n >= 64) ? n * n / 8 : ((n * n + 15) / 16) * 16;
   }
   p.s_off = off;
   off += ((MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS * 4 + 15) / 16 * 16;
@@ -58,13 +66,14 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0) {
   off += p.Ecap * 8;
   p.scr_off = off;
   off += 8 * 64 * 4;
-  p.pl_off = p.q_off = -1;
-  if (L >= 64) {  // bit-sliced sweeps (mcrg_resident_bits.cuh)
-    off = (off + 15) / 16 * 16;
-    p.pl_off = off;
-    off += 2 * (L * L / 64) * 4 + 16;  // planes + qn[2] (padded)
+  p.qn_off = p.q_off = -1;
+  if (planes) {
+    off = (off + 15) / 16 * 16;  // the queue holds uint4 entries
+    p.qn_off = off;
+    off += 16;
     p.q_off = off;
-    off += (L * L / 256 > 32 ? L * L / 256 : 32) * 16;
+    const int q = L * L / 256;
+    off += (q < 32 ? 32 : (q > 2048 ? 2048 : q)) * 16;  // resident::queue_cap(L)
   }
   p.bytes = (off + 15) / 16 * 16;
   return p;
@@ -75,9 +84,10 @@ inline int moment_entries(int n_levels, int C) { return (n_levels + 1) * C + 2 *
 // Host: acceptance parameters for coupling K (FP64, see include/mcrg.h).
 Accept make_accept(double K);
 
-// Launch `n_jobs` chains (all with the same L and threads; n_levels and C
-// bound the shared memory of every job).
-cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads,
+// Launch `n_jobs` chains (all with the same L, threads and acceptance regime:
+// `planes` = acc.fast && L >= 64; n_levels and C bound the shared memory of
+// every job).
+cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
                          cudaStream_t stream);
 
 // Stateless helpers on a device lattice in split layout (used by

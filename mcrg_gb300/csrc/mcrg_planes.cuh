@@ -38,6 +38,31 @@ __device__ __forceinline__ uint32_t left_sites(uint32_t x, uint32_t xp) {
   return (x << 8) | ((x >> 23) & 0xFEu) | (xp >> 31);
 }
 
+// Rotates the 5-bit bit index right by one: the bits at even positions go to
+// the low half in order, the odd ones to the high half (outer perfect
+// unshuffle, four delta swaps).
+__device__ __forceinline__ uint32_t unshuffle(uint32_t x) {
+  uint32_t t;
+  t = (x ^ (x >> 1)) & 0x22222222u; x ^= t ^ (t << 1);
+  t = (x ^ (x >> 2)) & 0x0C0C0C0Cu; x ^= t ^ (t << 2);
+  t = (x ^ (x >> 4)) & 0x00F000F0u; x ^= t ^ (t << 4);
+  t = (x ^ (x >> 8)) & 0x0000FF00u; x ^= t ^ (t << 8);
+  return x;
+}
+
+// Natural bit order (bit p = site p) -> plane order (bit pos(p)): pos(p)
+// rotates the index of p right by two.
+__device__ __forceinline__ uint32_t nat_to_plane(uint32_t v) { return unshuffle(unshuffle(v)); }
+
+// Bit-sliced count of four words: ge3 = at least three bits set, eq2 = exactly two.
+__device__ __forceinline__ void majority4(uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t& ge3,
+                                          uint32_t& eq2) {
+  const uint32_t s1 = a ^ b, c1 = a & b, s2 = c ^ d, c2 = c & d;
+  const uint32_t lo = s1 ^ s2, any2 = c1 | c2 | (s1 & s2), both = c1 & c2;
+  ge3 = both | (any2 & lo);
+  eq2 = any2 & ~both & ~lo;
+}
+
 // Bit-sliced update of 32 sites t from their neighbours u, d (other colour,
 // rows above and below), mid (same byte index) and side (the other
 // horizontal neighbour).  tz / to: the top bytes of thr[0] / thr[1] as

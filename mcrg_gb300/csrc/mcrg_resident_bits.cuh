@@ -1,9 +1,10 @@
-// mcrg_resident_bits.cuh -- bit-sliced sweeps of a shared-memory-resident
-// lattice (64 <= L <= 256), the same update and draws as the HBM sweep.
+// mcrg_resident_bits.cuh -- bit-sliced chains of a shared-memory-resident
+// lattice (64 <= L <= 1024, fast acceptance regime): sweeps, coupling sums
+// and b=2 majority blocking on plane words (mcrg_planes.cuh), the same update,
+// draws and measurement as the byte and HBM paths.
 //
-// The chain keeps a plane-word copy of level 0 (mcrg_planes.cuh) next to the
-// byte lattice: sweeps run on the planes, and the bytes are refreshed from
-// them before every measurement (blocking and coupling sums read bytes).  A
+// Every level of side m >= 64 lives only as plane words (m^2 / 8 bytes), so
+// an L = 1024 chain with all its levels fits one CTA's shared memory.  A
 // colour pass updates every plane word of the colour from the other colour's
 // words; words with open sites (8-bit draw equal to the threshold's top byte,
 // ~0.1 per word at Kc) are appended to a shared-memory queue and, after a
@@ -17,11 +18,128 @@
 namespace mcrg {
 namespace resident {
 
-// Queue entries of one colour pass: a quarter of the words (overflow is
-// decided by the word's owner).
-__host__ __device__ inline int queue_cap(int L) { return L * L / 256 > 32 ? L * L / 256 : 32; }
+// Queue entries of one colour pass: a quarter of the words, 32 .. 2048
+// (overflow is decided by the word's owner).
+__host__ __device__ inline int queue_cap(int L) {
+  const int q = L * L / 256;
+  return q < 32 ? 32 : (q > 2048 ? 2048 : q);
+}
 
-// byte lattice (split layout) -> plane words, colour c at pl + c * L * L / 64
+__device__ __forceinline__ int log2_words(int wpr) {
+  int lw = 0;
+  while ((1 << lw) < wpr) ++lw;
+  return lw;
+}
+
+// Initial coin (P_INIT) straight into plane words: site k of (colour c, row i)
+// is bit k & 31 of word (k & 127) >> 5 of block (row i, group k >> 7, sub c).
+__device__ __forceinline__ void init_planes(uint32_t* pl, int L, Key key, uint32_t rep, int tid, int T) {
+  const int wpr = L / 64, lw = log2_words(wpr), words = L * wpr;
+  for (int x = tid; x < 2 * words; x += T) {
+    const int c = x >= words, r = x - c * words, i = r >> lw, w = r & (wpr - 1);
+    const uint4 b = stream_block(key, rep, P_INIT, (uint32_t)c, (uint32_t)i, (uint32_t)(w >> 2), 0u);
+    pl[x] = planes::nat_to_plane(u4get(b, w & 3));
+  }
+}
+
+// Coupling sums of a plane level of side m >= 64 (the directional forms of
+// couplings_vec: down / right bonds of every site, each counted from one end
+// and scaled by two).  NC: couplings wanted (1..5).
+template <int NC>
+__device__ __forceinline__ void couplings_planes(const uint32_t* P, int m, int tid, int T, int (&acc)[5]) {
+  using planes::right_sites;
+  using planes::left_sites;
+  const int wpr = m / 64, lw = log2_words(wpr), words = m * wpr;
+  int a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, nw = 0;
+  for (int x = tid; x < 2 * words; x += T) {
+    const int c = x >= words, r = x - c * words, i = r >> lw, w = r & (wpr - 1);
+    const bool q = ((i + c) & 1) != 0;
+    const uint32_t* Cc = P + (size_t)c * words;
+    const uint32_t* Oc = P + (size_t)(1 - c) * words;
+    const int wn = (w + 1) & (wpr - 1), wp = (w - 1) & (wpr - 1);
+    const int r0 = i * wpr, r1 = ((i + 1) & (m - 1)) * wpr;
+    const uint32_t xv = Cc[r0 + w];
+    const uint32_t od = Oc[r1 + w];                                   // O[i+1][k]
+    const uint32_t oi = Oc[r0 + w], oin = Oc[r0 + wn];
+    const uint32_t oi1 = right_sites(oi, oin);                        // O[i][k+1]
+    const uint32_t oiq = q ? oi1 : oi;                                 // O[i][k+q]
+    a0 += __popc(xv ^ od) + __popc(xv ^ oiq);
+    uint32_t cdq = 0, ci1 = 0, cd2 = 0;
+    if (NC > 1) {
+      const uint32_t cd = Cc[r1 + w];
+      cdq = q ? right_sites(cd, Cc[r1 + wn]) : cd;                    // C[i+1][k+q]
+      const uint32_t cdqm = q ? cd : left_sites(cd, Cc[r1 + wp]);     // C[i+1][k+q-1]
+      a1 += __popc(xv ^ cdq) + __popc(xv ^ cdqm);
+    }
+    if (NC > 2) {
+      cd2 = Cc[((i + 2) & (m - 1)) * wpr + w];                        // C[i+2][k]
+      ci1 = right_sites(xv, Cc[r0 + wn]);                             // C[i][k+1]
+      a2 += __popc(xv ^ cd2) + __popc(xv ^ ci1);
+    }
+    if (NC > 3) a3 += __popc(xv ^ od ^ oiq ^ cdq);
+    if (NC > 4) {
+      const uint32_t oiq1 = q ? right_sites(oi1, oin >> 8) : oi1;     // O[i][k+q+1]
+      const uint32_t od3 = Oc[((i + 3) & (m - 1)) * wpr + w];         // O[i+3][k]
+      a4 += __popc(xv ^ oiq ^ ci1 ^ oiq1) + __popc(xv ^ od ^ cd2 ^ od3);
+    }
+    ++nw;
+  }
+  acc[0] += 128 * nw - 4 * a0;
+  if (NC > 1) acc[1] += 128 * nw - 4 * a1;
+  if (NC > 2) acc[2] += 128 * nw - 4 * a2;
+  if (NC > 3) acc[3] += 32 * nw - 2 * a3;
+  if (NC > 4) acc[4] += 64 * nw - 2 * a4;
+}
+
+// b = 2 majority blocking of a plane level of side m >= 64 into level m/2:
+// plane words when m/2 >= 64, split-layout bytes when m == 64.  Block (ib, jb)
+// counts split column jb of rows 2ib, 2ib+1 in both colours (bit pos(jb & 31)
+// of word jb >> 5); a tie takes bit jb & 31 of word (jb & 127) >> 5 of the
+// P_TIE block (level_out, ib, jb >> 7, sample), as block_vec does.  Output
+// (ib, jb) has colour (ib + jb) & 1 and split index jb >> 1: the bits of one
+// parity of two neighbouring input words form one output word, which is the
+// index rotation `unshuffle` once the parity is moved to index bit 3.
+__device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* out, Key key, uint32_t rep,
+                                             int level_out, uint32_t sample, int tid, int T) {
+  const int wpr = m / 64, words = m * wpr, h = m / 2;
+  const uint32_t* P0 = P;
+  const uint32_t* P1 = P + words;
+  if (h >= 64) {
+    uint32_t* Q = reinterpret_cast<uint32_t*>(out);
+    const int wpr1 = wpr / 2, lw1 = log2_words(wpr1), words1 = h * wpr1;
+    for (int x = tid; x < words1; x += T) {
+      const int ib = x >> lw1, w1 = x & (wpr1 - 1);
+      const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample);
+      uint32_t res[2];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int w = 2 * w1 + hh, ra = 2 * ib * wpr + w, rb = ra + wpr;
+        uint32_t ge3, eq2;
+        planes::majority4(P0[ra], P1[ra], P0[rb], P1[rb], ge3, eq2);
+        res[hh] = ge3 | (eq2 & planes::nat_to_plane(u4get(tb, w & 3)));
+      }
+      const uint32_t z0 = (res[0] & 0x00FF00FFu) | ((res[1] & 0x00FF00FFu) << 8);  // even jb
+      const uint32_t z1 = ((res[0] >> 8) & 0x00FF00FFu) | (res[1] & 0xFF00FF00u);  // odd jb
+      Q[(size_t)(ib & 1) * words1 + x] = planes::unshuffle(z0);
+      Q[(size_t)((ib + 1) & 1) * words1 + x] = planes::unshuffle(z1);
+    }
+  } else {  // m == 64: 32 rows of one word per colour -> bytes of side 32 (16 per colour row)
+    for (int ib = tid; ib < 32; ib += T) {
+      const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, 0u, sample);
+      uint32_t ge3, eq2;
+      planes::majority4(P0[2 * ib], P1[2 * ib], P0[2 * ib + 1], P1[2 * ib + 1], ge3, eq2);
+      const uint32_t res = ge3 | (eq2 & planes::nat_to_plane(tb.x));
+#pragma unroll
+      for (int par = 0; par < 2; ++par) {
+        uint4 a, b;
+        planes::unpack_bytes(planes::unshuffle((res >> (8 * par)) & 0x00FF00FFu), a, b);  // sites 0..15 in a
+        *reinterpret_cast<uint4*>(out + (size_t)((ib + par) & 1) * 32 * 16 + (size_t)ib * 16) = a;
+      }
+    }
+  }
+}
+
+// byte lattice (split layout, shared or global memory) -> plane words, colour c at pl + c * L * L / 64
 __device__ __forceinline__ void pack_lattice(const uint8_t* lat, uint32_t* pl, int L, int tid, int T) {
   const int words = L * L / 64;  // per colour; word r covers bytes 32r .. 32r + 31 of the colour array
   for (int x = tid; x < 2 * words; x += T) {
@@ -60,9 +178,7 @@ __device__ __forceinline__ uint32_t open_flips(Key key, uint32_t rep, const Acce
 // caller clears it again once the other colour's pass has started.
 __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_t t, Key key, uint32_t rep,
                                              const Accept& a, int tid, int T, uint4* q, int* qn) {
-  const int wpr = L / 64, words = L * wpr, cap = queue_cap(L);
-  int lw = 0;
-  while ((1 << lw) < wpr) ++lw;
+  const int wpr = L / 64, words = L * wpr, cap = queue_cap(L), lw = log2_words(wpr);
   uint32_t* Cc = pl + (size_t)c * words;
   const uint32_t* Oc = pl + (size_t)(1 - c) * words;
   uint32_t tz[8], to[8];

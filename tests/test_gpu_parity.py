@@ -225,6 +225,22 @@ def test_batch_equals_single_contexts(M, use_graph):
         assert_moments_equal(mom, solo(M, r))
 
 
+@pytest.mark.parametrize("L,C,nl", [(64, 3, -1), (128, 5, 2), (256, 4, -1), (512, 5, -1), (1024, 2, -1),
+                                    (1024, 5, 4)])
+def test_batch_resident_planes_matches_oracle(M, L, C, nl):
+    """Fast-regime chains up to MCRG_RESIDENT_MAX_L run shared-memory resident, every level
+    of side >= 64 as bit planes (sweeps, coupling sums and blocking on planes): the moments
+    equal the oracle's chain, bin for bin."""
+    nlv = int(math.log2(L)) - 1 if nl < 0 else nl
+    reqs = [M.make_request(L, K, seed=40 + i, replica=i, n_eq=3, n_samples=3, sweeps_between=1 + i % 2,
+                           n_levels=nl, n_couplings=C) for i, K in enumerate((KC, -0.47))]
+    res = M.batch_run(reqs)
+    for r, (st, mom) in zip(reqs, res):
+        assert st == 0
+        trace, _ = O.chain(L, r.K, C, nlv, r.seed, r.replica, n_eq=3, n_samples=3, sweeps_between=r.sweeps_between)
+        assert_moments_equal(mom, MomentSums.from_trace(trace))
+
+
 def test_server_alone_and_in_the_mix(M):
     reqs = mixed_requests(M)
     srv = M.Server(slots=8, hbm_budget_bytes=64 << 20)
@@ -247,16 +263,20 @@ def test_server_alone_and_in_the_mix(M):
 
 
 def test_server_hbm_requests_in_the_mix(M):
-    """HBM-size requests (L > 256) run on the server's worker pool, several with the same L
-    so that cached contexts are re-initialised between requests; every result equals the
-    single-context run of the same request, alone and while small requests run."""
+    """Requests too large for a resident chain (L = 2048) or outside the fast acceptance
+    regime (K = -0.1, L = 64) run on the server's worker pool, several with the same L so
+    that cached contexts are re-initialised between requests; L = 512 / 1024 in the fast
+    regime run as resident plane chains.  Every result equals the single-context run of the
+    same request, alone and while the others run."""
     rng = np.random.default_rng(5)
     reqs = []
     for i in range(14):
-        L = int(rng.choice([512, 1024])) if i % 2 == 0 else int(rng.choice([16, 64, 256]))
-        reqs.append(M.make_request(L, float(rng.uniform(-0.49, -0.43)), seed=300 + i, replica=i,
+        L = int(rng.choice([512, 1024, 2048])) if i % 2 == 0 else int(rng.choice([16, 64, 256]))
+        K = -0.1 if i == 5 else float(rng.uniform(-0.49, -0.43))
+        reqs.append(M.make_request(L, K, seed=300 + i, replica=i,
                                    n_eq=int(rng.integers(0, 4)), n_samples=int(rng.integers(1, 4)),
                                    sweeps_between=int(rng.integers(1, 3)), n_couplings=int(rng.choice([2, 5]))))
+    reqs[2] = M.make_request(2048, -0.45, seed=302, replica=2, n_eq=1, n_samples=2, n_couplings=5)
     srv = M.Server(slots=6, hbm_budget_bytes=1 << 30)
     try:
         tickets = [srv.submit(r) for r in reqs]
