@@ -51,7 +51,7 @@ int resident_threads(int L) {
   if (L <= 32) return 32;
   if (L == 64) return 64;
   if (L == 128) return 128;
-  return 256;
+  return L >= 512 ? 512 : 256;
 }
 
 void add_into(mcrg_moments* dst, const mcrg_moments* src) {

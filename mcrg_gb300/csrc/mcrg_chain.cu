@@ -43,7 +43,10 @@ __device__ __forceinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key
 // ---------------------------------------------------------------------------
 // One chain per CTA.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) chain_kernel(const ChainJob* __restrict__ jobs) {
+// MAXT / MINB: launch bounds of the instantiation (256 x 3 for L <= 256, 512 x 2
+// for the plane chains of L >= 512, which run one or two CTAs per SM).
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __restrict__ jobs) {
   extern __shared__ __align__(16) uint8_t smem[];
   const ChainJob& J = jobs[blockIdx.x];
   const int L = J.L, nl = J.n_levels, C = J.C;
@@ -214,14 +217,19 @@ cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels
                          cudaStream_t stream) {
   const SmemPlan plan = make_plan(L, n_levels, C, planes);
   constexpr int kMaxSmem = 227 * 1024;  // opt-in shared memory per CTA
-  if (plan.bytes > kMaxSmem) return cudaErrorInvalidValue;
-  static int configured = 0;  // per process: the attribute is per function, set once for the largest plan
-  if (plan.bytes > 48 * 1024 && configured < kMaxSmem) {
-    cudaError_t e = cudaFuncSetAttribute(chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+  if (plan.bytes > kMaxSmem || threads > 512) return cudaErrorInvalidValue;
+  const bool wide = threads > 256;
+  static bool configured[2] = {false, false};  // the attribute is per instantiation, set once to the maximum
+  if (plan.bytes > 48 * 1024 && !configured[wide]) {
+    cudaError_t e = wide ? cudaFuncSetAttribute(chain_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kMaxSmem)
+                         : cudaFuncSetAttribute(chain_kernel<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kMaxSmem);
     if (e != cudaSuccess) return e;
-    configured = kMaxSmem;
+    configured[wide] = true;
   }
-  chain_kernel<<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
+  if (wide) chain_kernel<512, 2><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
+  else chain_kernel<256, 3><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
   return cudaGetLastError();
 }
 
