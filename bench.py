@@ -205,7 +205,7 @@ def run_large(args, D: Dist) -> dict:
     peak, kind = peaks()
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
     tile = lat.tile_shape()
-    kname = "bits_sweep_b%d" % tile[1]
+    kname = "bits_sweep_b%d_r%d" % (tile[1], tile[0])  # threads per CTA, rows per group
     traffic = profiled_traffic(kname)
 
     # ---- end to end through the C ABI with host buffers
