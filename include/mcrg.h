@@ -37,6 +37,14 @@
  *          u32 = r8<<24 | r24;
  *   ties   purpose 4, sub = level produced, row = ib, group = jb>>7,
  *          time = sample index: tie value = bit (jb&127) ? +1 : -1.
+ *   bonds  purpose 5 (cluster updates), row = i, group = j>>1, time = update
+ *          index t: the bond of site (i, j) to (i, j+1) draws word 2*(j&1),
+ *          the bond to (i+1, j) word 2*(j&1)+1; a bond is open iff both
+ *          spins are equal and the word is below floor((1 - exp(2K)) 2^32);
+ *   cluster purpose 6, time = t: Wolff seed site i*L + j = word 0 of block
+ *          (row 0, sub 0, group 0) mod L^2; Swendsen-Wang flips the
+ *          cluster whose smallest site index is r iff bit 0 of word 0 of
+ *          block (row r>>16, sub 1, group r & 0xFFFF) is set.
  * Site (i, j) has colour c = (i+j)&1 and split index k = j>>1.  Colour 0 is
  * updated before colour 1 within a sweep.
  *
@@ -183,6 +191,30 @@ int mcrg_rgnn_scalar_output(mcrg_ctx* ctx, const double W[4], double* out);
  * (src/mcrg.cpp:283-301) combines the moments of a context of side L and one
  * of side L/b at the same K. */
 int mcrg_measure_flow(mcrg_ctx* ctx, int64_t n_samples, int64_t sweeps_between, mcrg_flow_moments* out);
+
+/* Cluster updates on the device: the reference's own update rule
+ * (IsingModel::sample_new_configuration, src/ising.cpp:87-155: one Wolff
+ * cluster grown from a random site through aligned nearest neighbours, each
+ * bond open with probability 1 - exp(2K) (src/ising.cpp:9), then flipped) and
+ * its all-cluster form (Swendsen-Wang: every cluster of the same bond
+ * configuration flipped with probability 1/2).  A Wolff cluster is the
+ * connected component of the seed under open bonds, so it is labelled
+ * order-independently (union-find) from per-bond draws of the stream above.
+ * Each update consumes one sweep index (the time word t); *flipped (may be
+ * NULL) receives the number of spins flipped over the n updates (for Wolff,
+ * the summed cluster sizes).  kind: MCRG_UPDATE_WOLFF or
+ * MCRG_UPDATE_SWENDSEN_WANG.  The first call allocates 4 L^2 bytes of
+ * labels for the context. */
+enum { MCRG_UPDATE_WOLFF = 1, MCRG_UPDATE_SWENDSEN_WANG = 2 };
+int mcrg_cluster_update(mcrg_ctx* ctx, int64_t n, int32_t kind, int64_t* flipped);
+
+/* mcrg_measure with cluster updates in place of sweeps: n_samples x
+ * (updates_between cluster updates of the given kind, then blocking + coupling
+ * sums at every level + moment accumulation) -- the sample loop of
+ * calc_critical_exponent (src/mcrg.cpp:72-98) with the reference's update
+ * rule. */
+int mcrg_measure_cluster(mcrg_ctx* ctx, int64_t n_samples, int64_t updates_between, int32_t kind,
+                         mcrg_moments* total, int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap);
 
 /* Sweep and sample counters (the Philox time words of the next sweep / sample). */
 int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);

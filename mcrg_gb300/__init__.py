@@ -128,6 +128,28 @@ class Lattice:
         check(lib().mcrg_measure(self._ctx, n_samples, sweeps_between, C.byref(tot), 0, None, 0), "mcrg_measure")
         return moments_from_c(tot), []
 
+    def cluster_update(self, n: int = 1, kind: str = "wolff") -> int:
+        """n cluster updates on the device: "wolff" (the reference's update rule,
+        src/ising.cpp:87-155) or "sw" (Swendsen-Wang); returns the spins flipped."""
+        f = C.c_int64()
+        check(lib().mcrg_cluster_update(self._ctx, n, _cluster_kind(kind), C.byref(f)), "mcrg_cluster_update")
+        return int(f.value)
+
+    def measure_cluster(self, n_samples: int, updates_between: int = 1, kind: str = "wolff", bin_size: int = 0):
+        """measure() with cluster updates in place of sweeps: the sample loop of
+        src/mcrg.cpp:72-98 with the reference's update rule; returns (total, bins)."""
+        tot = _abi.Moments()
+        k = _cluster_kind(kind)
+        if bin_size > 0:
+            nb = (n_samples + bin_size - 1) // bin_size
+            bins = (_abi.Moments * nb)()
+            check(lib().mcrg_measure_cluster(self._ctx, n_samples, updates_between, k, C.byref(tot), bin_size, bins,
+                                             nb), "mcrg_measure_cluster")
+            return moments_from_c(tot), [moments_from_c(b) for b in bins]
+        check(lib().mcrg_measure_cluster(self._ctx, n_samples, updates_between, k, C.byref(tot), 0, None, 0),
+              "mcrg_measure_cluster")
+        return moments_from_c(tot), []
+
     def measure_flow(self, n_samples: int, sweeps_between: int = 1):
         """Flow moments (src/mcrg.cpp:225-258 for one lattice): sums of S_nn per level
         and of S_nn(level) * S_nn(level 0), exact integers."""
@@ -263,6 +285,17 @@ def lattice_couplings(spins: np.ndarray, n_couplings: int = 5, device: int = 0) 
     out = (C.c_int64 * n_couplings)()
     check(lib().mcrg_lattice_couplings(s.shape[0], _ptr(s), n_couplings, out, device), "mcrg_lattice_couplings")
     return np.array(list(out), dtype=np.int64)
+
+
+UPDATE_WOLFF, UPDATE_SWENDSEN_WANG = 1, 2
+
+
+def _cluster_kind(kind) -> int:
+    if kind in ("wolff", UPDATE_WOLFF):
+        return UPDATE_WOLFF
+    if kind in ("sw", "swendsen-wang", UPDATE_SWENDSEN_WANG):
+        return UPDATE_SWENDSEN_WANG
+    raise ValueError("cluster update kind: 'wolff' or 'sw'")
 
 
 def make_request(L: int, K: float, seed: int, replica: int = 0, n_eq: int = 0, n_samples: int = 0,

@@ -82,6 +82,9 @@ _SIGS = {
     "mcrg_interactions": (C.c_int, [C.c_void_p, P(C.c_int64)]),
     "mcrg_measure": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(Moments), C.c_int64, P(Moments), C.c_int64]),
     "mcrg_measure_flow": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(FlowMoments)]),
+    "mcrg_cluster_update": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, P(C.c_int64)]),
+    "mcrg_measure_cluster": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, P(Moments), C.c_int64,
+                                       P(Moments), C.c_int64]),
     "mcrg_rgnn_scalar_output": (C.c_int, [C.c_void_p, P(C.c_double), P(C.c_double)]),
     "mcrg_counters": (C.c_int, [C.c_void_p, P(C.c_uint64), P(C.c_uint64)]),
     "mcrg_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),

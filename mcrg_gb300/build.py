@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmcrg.so")
-UNITS = ["mcrg_chain.cu", "mcrg_tiled.cu", "mcrg_capi.cu", "mcrg_batch.cu", "mcrg_noalloc.cu", "mcrg_rgnn.cu"]
+UNITS = ["mcrg_chain.cu", "mcrg_tiled.cu", "mcrg_capi.cu", "mcrg_batch.cu", "mcrg_noalloc.cu", "mcrg_rgnn.cu",
+         "mcrg_cluster.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                      "--expt-relaxed-constexpr"]

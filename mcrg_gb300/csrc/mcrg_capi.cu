@@ -34,6 +34,8 @@ struct mcrg_ctx {
   int* d_flag = nullptr;
   Accept acc;
   double* d_rgnn = nullptr;     // forward-pass work: (L/32)^2 + (L/1024)^2 + 3 doubles, the last one the result
+  int* d_labels = nullptr;      // cluster updates: L^2 labels (allocated by the first update)
+  unsigned long long* d_cl = nullptr;  // cluster updates: [0] flipped spins, [1] error flags
 };
 
 namespace {
@@ -284,6 +286,8 @@ int mcrg_free(mcrg_ctx* c) {
   cudaFree(c->d_nat);
   cudaFree(c->d_flag);
   cudaFree(c->d_rgnn);
+  cudaFree(c->d_labels);
+  cudaFree(c->d_cl);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MCRG_OK;
@@ -380,6 +384,83 @@ static int measure_impl(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, 
 int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total, int64_t bin_size,
                  mcrg_moments* bins, int64_t n_bins_cap) {
   return measure_impl(c, n_samples, sweeps_between, total, bin_size, bins, n_bins_cap, false);
+}
+
+// n cluster updates at update indices c->t, c->t + 1, ...; queued on the
+// context's stream.  The flipped count accumulates in c->d_cl[0].
+static int cluster_updates(mcrg_ctx* c, int64_t n, int32_t kind) {
+  const int L = c->cfg.L;
+  if (!c->d_labels) {
+    if (cudaMalloc(&c->d_labels, sizeof(int) * (size_t)L * L) != cudaSuccess) return MCRG_ENOMEM;
+    if (cudaMalloc(&c->d_cl, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaFree(c->d_labels);
+      c->d_labels = nullptr;
+      return MCRG_ENOMEM;
+    }
+    CK(cudaMemsetAsync(c->d_cl, 0, 2 * sizeof(unsigned long long), c->stream));
+  }
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->cfg.device));
+  uint8_t* st = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
+  const Key key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
+  const uint32_t tb = bond_threshold(c->cfg.K);
+  int* err = reinterpret_cast<int*>(c->d_cl + 1);
+  for (int64_t k = 0; k < n; ++k)
+    CK(launch_cluster_update(st, L, c->d_labels, kind, key, c->cfg.replica, (uint32_t)(c->t + (uint64_t)k), tb,
+                             c->d_cl, err, sms, c->stream));
+  c->t += (uint64_t)n;
+  return MCRG_OK;
+}
+
+// Reads and clears the flipped count and the error flags of the cluster kernels.
+static int cluster_readback(mcrg_ctx* c, int64_t* flipped) {
+  unsigned long long h[2] = {0, 0};
+  if (c->d_cl) {
+    CK(cudaMemcpyAsync(h, c->d_cl, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->d_cl, 0, sizeof h, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  if (flipped) *flipped = (int64_t)h[0];
+  return h[1] ? MCRG_EIO : MCRG_OK;
+}
+
+int mcrg_cluster_update(mcrg_ctx* c, int64_t n, int32_t kind, int64_t* flipped) {
+  if (!c || n < 0 || (kind != MCRG_UPDATE_WOLFF && kind != MCRG_UPDATE_SWENDSEN_WANG)) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  int rc = cluster_updates(c, n, kind);
+  if (rc) return rc;
+  return cluster_readback(c, flipped);
+}
+
+int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between, int32_t kind, mcrg_moments* total,
+                         int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap) {
+  if (!c || n_samples < 0 || updates_between < 0 ||
+      (kind != MCRG_UPDATE_WOLFF && kind != MCRG_UPDATE_SWENDSEN_WANG))
+    return MCRG_EINVAL;
+  if (bins && (bin_size <= 0 || n_bins_cap < 0)) return MCRG_EINVAL;
+  CK(cudaSetDevice(c->cfg.device));
+  const int nl = c->n_levels, C = c->cfg.n_couplings;
+  if (total) {
+    memset(total, 0, sizeof *total);
+    total->n_levels = nl;
+    total->n_couplings = C;
+  }
+  if (bins)
+    for (int64_t q = 0; q < n_bins_cap; ++q) {
+      memset(&bins[q], 0, sizeof bins[q]);
+      bins[q].n_levels = nl;
+      bins[q].n_couplings = C;
+    }
+  for (int64_t q = 0; q < n_samples; ++q) {
+    int rc = cluster_updates(c, updates_between, kind);
+    if (rc) return rc;
+    mcrg_moments m;  // one measurement, no sweeps (its readback synchronises the stream)
+    rc = measure_impl(c, 1, 0, &m, 0, nullptr, 0, false);
+    if (rc) return rc;
+    if (total) add_moments(total, &m);
+    if (bins && q / bin_size < n_bins_cap) add_moments(&bins[q / bin_size], &m);
+  }
+  return cluster_readback(c, nullptr);
 }
 
 int mcrg_measure_flow(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_flow_moments* out) {

@@ -96,6 +96,16 @@ cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const 
                               Key key, uint32_t replica, int level, uint32_t sample, cudaStream_t s);
 cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out, cudaStream_t s);
 
+// One cluster update (Wolff or Swendsen-Wang, mcrg_cluster.cu) of a split-
+// layout lattice of side L at update index t: d_label holds L^2 ints,
+// *d_count gains the number of flipped spins, *d_err gets bit 2 / 4 when a
+// find / union loop hits its bound.
+cudaError_t launch_cluster_update(uint8_t* d_state, int L, int* d_label, int kind, Key key, uint32_t replica,
+                                  uint32_t t, uint32_t bond_threshold, unsigned long long* d_count, int* d_err,
+                                  int num_sms, cudaStream_t s);
+// floor((1 - exp(2K)) 2^32), 0 when no bond can open (K >= 0).
+uint32_t bond_threshold(double K);
+
 // New chain on an HBM-resident context without allocating (mcrg_capi.cu).
 int reinit_context(mcrg_ctx* c, double K, uint64_t seed, uint32_t replica);
 

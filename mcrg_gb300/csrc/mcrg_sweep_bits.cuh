@@ -91,16 +91,18 @@ __device__ __forceinline__ uint4 draw(const Params& P, uint32_t purpose, uint32_
 // per colour.
 constexpr int kPackSlots = 8;          // plane-word groups held per colour
 // Open-site queue entries per buffer: one entry per plane word with open
-// sites (about 0.1 per word at the critical coupling); a word that finds its
-// buffer full is resolved by its owner.
-template <int NT>
+// sites (about 0.1 per word at the critical coupling, 51 +- 7 of 512); a word
+// that finds its buffer full is resolved by its owner.  The single-slot form
+// (LEAD = 0) keeps 5/32 of the words so that three 512-word CTAs fit an SM.
+template <int NT, int LEAD>
 constexpr int queue_cap() {
-  return NT / 4;
+  return LEAD == 0 ? NT * 5 / 32 : NT / 4;
 }
 
 template <int NT, int LEAD>
 constexpr size_t smem_bytes() {
-  return 128 + 6 * (size_t)queue_cap<NT>() * 16 + 2 * (size_t)(LEAD + 1) * NT * 32 + 2 * (size_t)kPackSlots * NT * 4;
+  return 128 + 6 * (size_t)queue_cap<NT, LEAD>() * 16 + 2 * (size_t)(LEAD + 1) * NT * 32 +
+         2 * (size_t)kPackSlots * NT * 4;
 }
 
 using planes::left_sites;
@@ -134,12 +136,13 @@ __device__ __forceinline__ uint32_t open_flips(const Params& P, uint32_t c, int 
 
 // Queues plane word w (band offset off) of colour c, which has open sites;
 // returns their flips when the buffer is full (resolved here), else 0.
-template <int NT>
+template <int NT, int LEAD>
 __device__ __forceinline__ uint32_t enqueue(uint32_t open, uint32_t zero, uint32_t t, int off, int w, int gr,
                                             int c, int qi, int* qn, uint4* Q, const Params& P, uint32_t tt) {
+  constexpr int CAP = queue_cap<NT, LEAD>();
   const int slot = atomicAdd(&qn[qi], 1);
-  if (slot < queue_cap<NT>()) {
-    Q[qi * queue_cap<NT>() + slot] = make_uint4(open, zero & open, t & open, ((uint32_t)off << 8) | (uint32_t)w);
+  if (slot < CAP) {
+    Q[qi * CAP + slot] = make_uint4(open, zero & open, t & open, ((uint32_t)off << 8) | (uint32_t)w);
     return 0u;
   }
   return open_flips(P, (uint32_t)c, gr, w, open, zero, tt);
@@ -194,7 +197,7 @@ __device__ __forceinline__ void resolve_queue(int c, int g, int first, int strid
                                               uint32_t* pk, uint8_t* out, int top, int ms, const Params& P,
                                               uint32_t tt) {
   using G = Geo<NT, LW, LEAD>;
-  constexpr int CAP = queue_cap<NT>();
+  constexpr int CAP = queue_cap<NT, LEAD>();
   const int qi = c * 3 + g % 3;
   const int n = min(qn[qi], CAP);
   for (int e = first; e < n; e += stride) {
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(NT, MINB)
   using G = Geo<NS, LW, LEAD>;
   constexpr int L = G::L, H = G::H, WPR = G::WPR, R = G::R, RAW_ROWS = G::RAW_ROWS, PK_ROWS = G::PK_ROWS;
   constexpr size_t PLANE = G::PLANE;
-  constexpr int kRawSlots = LEAD + 1, CAP = queue_cap<NS>();
+  constexpr int kRawSlots = LEAD + 1, CAP = queue_cap<NS, LEAD>();
   extern __shared__ __align__(128) uint8_t smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   int* qn = reinterpret_cast<int*>(smem + 64);                    // [colour][3] queue lengths
@@ -275,30 +278,38 @@ __global__ void __launch_bounds__(NT, MINB)
       if (STEADY || p >= 4) qn[(p - 4) % 3] = 0;
       if (STEADY || p >= 7) qn[3 + (p - 7) % 3] = 0;
     }
+    // ---- LEAD = 0: the copy of group p goes out first and lands while the
+    //      phase works on older groups; group p is packed at the end
+    if (LEAD == 0 && tid < 32 && (STEADY || p < J)) issue_group<NS, LW, LEAD>(p, top, b0, b1, ms, in, raw, bar, lane);
     // ---- open sites queued last phase: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6
     {
       const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
       if (STEADY || (g >= 0 && g < J))
         resolve_queue<NS, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
     }
-    // ---- bulk copies of group p + LEAD (its slot was packed last phase)
-    if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
-    // ---- pack group p
-    if (STEADY || p < J) {
-      if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
+    // ---- pack group p (waits for its copy)
+    auto pack_group = [&]() {
+      if (STEADY || p < J) {
+        if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
 #pragma unroll
-      for (int j = 0; j < WPT; ++j) {
-        const int w = wj[j], off = p * R + rj[j], x = top + off;
-        const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
-        if (STEADY || (x >= b0 - 1 && x <= b1)) {
-          const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
-          pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
-        }
-        if (STEADY || x <= b1 + 1) {
-          const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
-          pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+        for (int j = 0; j < WPT; ++j) {
+          const int w = wj[j], off = p * R + rj[j], x = top + off;
+          const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
+          if (STEADY || (x >= b0 - 1 && x <= b1)) {
+            const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
+            pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+          }
+          if (STEADY || x <= b1 + 1) {
+            const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
+            pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+          }
         }
       }
+    };
+    if (LEAD > 0) {
+      // ---- bulk copies of group p + LEAD (its slot was packed last phase)
+      if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
+      pack_group();
     }
     // ---- colour 0 of group p-2
 #pragma unroll
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(NT, MINB)
         const uint4 B = draw(P, P_SWEEP_HI, 0u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue<NS>(open, zero, t, off, w, gr, 0, (p - 2) % 3, qn, Q, P, tt);
+        if (open) nt ^= enqueue<NS, LEAD>(open, zero, t, off, w, gr, 0, (p - 2) % 3, qn, Q, P, tt);
         pk[pi * WPR + w] = nt;
       }
     }
@@ -338,7 +349,7 @@ __global__ void __launch_bounds__(NT, MINB)
         const uint4 B = draw(P, P_SWEEP_HI, 1u, (uint32_t)gr, (uint32_t)(2 * w + 1), tt);
         uint32_t open, zero;
         uint32_t nt = decide(t, u, d, mid, side, A, B, P, open, zero);
-        if (open) nt ^= enqueue<NS>(open, zero, t, off, w, gr, 1, 3 + (p - 5) % 3, qn, Q, P, tt);
+        if (open) nt ^= enqueue<NS, LEAD>(open, zero, t, off, w, gr, 1, 3 + (p - 5) % 3, qn, Q, P, tt);
         uint4 a, b;
         unpack_bytes(mid, a, b);
         uint4* o0 = reinterpret_cast<uint4*>(out + (size_t)gr * H + 32 * w);
@@ -350,6 +361,7 @@ __global__ void __launch_bounds__(NT, MINB)
         o1[1] = b;
       }
     }
+    if (LEAD == 0) pack_group();
   };
   // steady phases: groups p (pack), p-2, p-5 and the queues of p-3, p-6 all
   // lie inside the band with every row valid

@@ -168,7 +168,8 @@ struct Variant {
 const Variant kVariants[] = {BITS_VARIANT(256, 4, 1, 8),        BITS_VARIANT(256, 3, 2, 8),
                              BITS_VARIANT(256, 2, 3, 8),        BITS_VARIANT(512, 1, 3, 8),
                              BITS_VARIANT_X(128, 2, 4, 1, 8),    BITS_VARIANT_X(128, 2, 4, 2, 8),
-                             BITS_VARIANT_X(256, 2, 2, 1, 8),    BITS_VARIANTS_L(7),
+                             BITS_VARIANT_X(256, 2, 2, 1, 8),    BITS_VARIANT_X(256, 2, 3, 0, 8),
+                             BITS_VARIANT_X(128, 2, 6, 0, 8),    BITS_VARIANTS_L(7),
                              BITS_VARIANTS_L(6),                 BITS_VARIANTS_L(5),
                              BITS_VARIANTS_L(4),                 BITS_VARIANTS_L(3)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);

@@ -385,6 +385,84 @@ int64_t orc_wolff_steps(orc_wolff_t* w, int8_t* spins, int64_t n) {
     return flipped;
 }
 
+/* ------------------------------------------------------------------ */
+/* Cluster updates with the device's bond and cluster streams           */
+/* (include/mcrg.h).  The bond of (i,j) to (i,j+1) is word 2*(j&1), the */
+/* bond to (i+1,j) word 2*(j&1)+1 of the purpose-5 block (row i, group  */
+/* j>>1, time t); it is open iff both spins are equal and the word is   */
+/* below tb = floor((1 - exp(2K)) 2^32).  Clusters are labelled by a     */
+/* sequential union-find that keeps the smallest index as the root.     */
+/* kind 1 (Wolff): flip the component of the seed site, word 0 of the   */
+/* purpose-6 block (sub 0, row 0, group 0) mod N^2 -- the component the */
+/* reference's breadth-first step grows from that site with the same    */
+/* bond outcomes (src/ising.cpp:87-155).  kind 2 (Swendsen-Wang): flip  */
+/* every component whose root r draws bit 0 of word 0 of the purpose-6  */
+/* block (sub 1, row r>>16, group r&0xFFFF) set.  Returns the number of */
+/* flipped spins, -1 when out of memory.                                 */
+/* ------------------------------------------------------------------ */
+static int dsu_find(int* p, int x) {
+    while (p[x] != x) {
+        p[x] = p[p[x]];
+        x = p[x];
+    }
+    return x;
+}
+
+static void dsu_union(int* p, int a, int b) {
+    a = dsu_find(p, a);
+    b = dsu_find(p, b);
+    if (a == b) return;
+    if (a < b) p[b] = a;
+    else p[a] = b;
+}
+
+uint32_t orc_bond_threshold(double K) {
+    double p = 1.0 - exp(2.0 * K);
+    if (!(p > 0.0)) return 0u;
+    double x = floor(p * 4294967296.0);
+    return x >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)x;
+}
+
+int64_t orc_cluster_update(int N, int8_t* s, double K, uint64_t seed, uint32_t replica, uint32_t t, int kind) {
+    const uint32_t tb = orc_bond_threshold(K);
+    const int n = N * N;
+    int* par = (int*)malloc((size_t)n * sizeof(int));
+    signed char* dec = (signed char*)malloc((size_t)n);
+    if (!par || !dec) { free(par); free(dec); return -1; }
+    for (int x = 0; x < n; ++x) par[x] = x;
+    uint32_t w[4];
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; j += 2) {
+            stream(seed, replica, 5u, 0u, (uint32_t)i, (uint32_t)(j >> 1), t, w);
+            for (int d = 0; d < 2; ++d) {
+                const int jj = j + d, x = i * N + jj;
+                const int xr = i * N + (jj + 1) % N, xd = ((i + 1) % N) * N + jj;
+                if (w[2 * d] < tb && s[x] == s[xr]) dsu_union(par, x, xr);
+                if (w[2 * d + 1] < tb && s[x] == s[xd]) dsu_union(par, x, xd);
+            }
+        }
+    int64_t flipped = 0;
+    if (kind == 1) {
+        stream(seed, replica, 6u, 0u, 0u, 0u, t, w);
+        const int r0 = dsu_find(par, (int)(w[0] & (uint32_t)(n - 1)));
+        for (int x = 0; x < n; ++x)
+            if (dsu_find(par, x) == r0) { s[x] = (int8_t)-s[x]; ++flipped; }
+    } else {
+        memset(dec, -1, (size_t)n);
+        for (int x = 0; x < n; ++x) {
+            const int r = dsu_find(par, x);
+            if (dec[r] < 0) {
+                stream(seed, replica, 6u, 1u, (uint32_t)r >> 16, (uint32_t)r & 0xFFFFu, t, w);
+                dec[r] = (signed char)(w[0] & 1u);
+            }
+            if (dec[r]) { s[x] = (int8_t)-s[x]; ++flipped; }
+        }
+    }
+    free(par);
+    free(dec);
+    return flipped;
+}
+
 /* One measurement (all levels, Philox tie stream at `sample`). */
 int orc_measure(int N, const int8_t* spins, int C, int n_levels, uint64_t seed, uint32_t replica,
                 uint32_t sample, int64_t* S) {

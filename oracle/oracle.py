@@ -46,6 +46,10 @@ def lib() -> C.CDLL:
         h.orc_measure.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint32, C.c_uint32,
                                   P(C.c_int64)]
         h.orc_measure.restype = C.c_int
+        h.orc_cluster_update.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int]
+        h.orc_cluster_update.restype = C.c_int64
+        h.orc_bond_threshold.argtypes = [C.c_double]
+        h.orc_bond_threshold.restype = C.c_uint32
         _lib = h
     return _lib
 
@@ -151,6 +155,23 @@ def measure(spins: np.ndarray, C_: int, n_levels: int, seed: int, replica: int =
     return np.array(list(out), dtype=np.int64).reshape(n_levels + 1, C_)
 
 
+WOLFF, SWENDSEN_WANG = 1, 2
+
+
+def cluster_update(spins: np.ndarray, K: float, seed: int, replica: int = 0, t: int = 0, kind: int = WOLFF,
+                   n: int = 1):
+    """(spins after n cluster updates at update indices t .. t+n-1, flipped spins per update)
+    with the device's bond / cluster streams."""
+    s = np.ascontiguousarray(spins, dtype=np.int8).copy()
+    flips = []
+    for k in range(n):
+        f = lib().orc_cluster_update(s.shape[0], _p(s), K, seed, replica, t + k, kind)
+        if f < 0:
+            raise MemoryError("orc_cluster_update")
+        flips.append(int(f))
+    return s, flips
+
+
 def exact4(K: float, C_: int = 2) -> dict:
     n = 2 + 2 * C_ + 2 * C_ * C_
     out = (C.c_double * n)()
@@ -206,6 +227,8 @@ def ref_lib() -> C.CDLL | None:
         h.ref_equilibrate_log.restype = C.c_int
         h.ref_rgnn_scalar_output.argtypes = [C.c_int, C.c_void_p, P(C.c_double)]
         h.ref_rgnn_scalar_output.restype = C.c_double
+        h.ref_wolff_sizes.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        h.ref_wolff_sizes.restype = C.c_int
         _ref = h
     return _ref
 

@@ -187,6 +187,32 @@ int ref_equilibrate_log(uint64_t seed, int N, double K, int n, const char* dir) 
 // RenormalizationGroupNeuralNetwork::scalar_output (src/rgnn.cpp:281-307)
 // of a +-1 lattice (row-major, site (i, j) at i*N + j = spins_(i, j)) with
 // weights W(r, k) = W[2r + k].
+// The reference's own Wolff step (IsingModel::sample_new_configuration,
+// src/ising.cpp:87-155) on a fresh Lattice(N) after rng.seed(seed): n_eq steps,
+// then per step s < n_steps the number of spins it flipped (sizes[s]) and the
+// bond sum sum_(i,j) s(i,j) (s(i+1,j) + s(i,j+1)) after it (bonds[s]).
+int ref_wolff_sizes(uint64_t seed, int N, double K, int n_eq, int n_steps, int32_t* sizes, int32_t* bonds) {
+    rng.seed(seed);
+    IsingModel ising(K);
+    std::shared_ptr<Lattice> lat(new Lattice(N));
+    for (int s = 0; s < n_eq; ++s) ising.sample_new_configuration(lat);
+    imat prev = lat->spins_;
+    for (int s = 0; s < n_steps; ++s) {
+        ising.sample_new_configuration(lat);
+        int changed = 0, b = 0;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                const int v = lat->spins_(i, j);
+                changed += v != prev(i, j);
+                b += v * (lat->spins_((i + 1) % N, j) + lat->spins_(i, (j + 1) % N));
+            }
+        sizes[s] = changed;
+        bonds[s] = b;
+        prev = lat->spins_;
+    }
+    return 0;
+}
+
 double ref_rgnn_scalar_output(int N, const int8_t* spins, const double* W) {
     imat s(N, N);
     for (int i = 0; i < N; ++i)

@@ -13,7 +13,9 @@ compiled into oracle/_ref/libmcrg_ref.so by oracle/build.py) and records:
                    seed, plus the largest eigenvalues it printed for the same
                    seed;
   ref_stats.npz    the reference's own Wolff-chain estimates at L = 8, K = Kc
-                   (mean and spread over seeds) for the statistical checks.
+                   (mean and spread over seeds) for the statistical checks;
+  ref_wolff.npz    mean cluster size and bond sum per Wolff step of the
+                   reference (`python tests/golden/make_golden.py wolff`).
 
 Needs the mounted reference sources; the fixtures are committed so the GPU
 box (which has no reference) can use them.  Usage:
@@ -158,9 +160,31 @@ def main_rgnn():
     print("rgnn outputs", outs[:6])
 
 
+def main_wolff():
+    """The reference's own Wolff step (src/ising.cpp:87-155): per (L, K) and seed, the
+    mean cluster size and mean bond sum per step of one chain (independent seeds, so
+    their spread gives honest error bars; the steps of one chain are correlated)."""
+    R = O.ref_lib()
+    Ls, Ks, n_seeds, n_eq, n_steps = (8, 16, 32), (KC, -0.40, -0.50), 5, 2000, 20000
+    size = np.zeros((len(Ls), len(Ks), n_seeds))
+    bond = np.zeros_like(size)
+    for a, L in enumerate(Ls):
+        for b, K in enumerate(Ks):
+            for k in range(n_seeds):
+                sz = np.empty(n_steps, dtype=np.int32)
+                bd = np.empty(n_steps, dtype=np.int32)
+                R.ref_wolff_sizes(7000 + 100 * a + 10 * b + k, L, K, n_eq, n_steps, p(sz), p(bd))
+                size[a, b, k], bond[a, b, k] = sz.mean(), bd.mean()
+            print("L=%d K=%.5f <size> %s <bonds> %s" % (L, K, size[a, b].round(2), bond[a, b].round(2)))
+    np.savez_compressed(os.path.join(HERE, "ref_wolff.npz"), L=np.array(Ls), K=np.array(Ks), n_eq=n_eq,
+                        n_steps=n_steps, size=size, bond=bond)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["rgnn"]:
         main_rgnn()
+    elif sys.argv[1:] == ["wolff"]:
+        main_wolff()
     elif sys.argv[1:] == ["critical"]:
         main_critical()
     elif sys.argv[1:] == ["equilibrate"]:

@@ -1,0 +1,198 @@
+"""Cluster updates (Wolff / Swendsen-Wang; the reference's update rule,
+src/ising.cpp:87-155): the device's union-find labelling against the oracle
+bit for bit, and the update rule against the reference's own Wolff step
+statistically (tests/golden/ref_wolff.npz, written by make_golden.py wolff)."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from mcrg_gb300.tmatrix import MomentSums
+from tests.helpers import KC
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ref_wolff.npz")
+KIND = {"wolff": O.WOLFF, "sw": O.SWENDSEN_WANG}
+
+
+def bond_sum(s: np.ndarray) -> int:
+    s = s.astype(np.int64)
+    return int((s * (np.roll(s, -1, 0) + np.roll(s, -1, 1))).sum())
+
+
+def within(ours: np.ndarray, ref: np.ndarray, nsig: float = 5.0) -> bool:
+    """Means of independent chains agree within nsig combined standard errors."""
+    se = math.sqrt(ours.var(ddof=1) / len(ours) + ref.var(ddof=1) / len(ref))
+    return abs(ours.mean() - ref.mean()) < nsig * se + 1e-9
+
+
+# --------------------------------------------------------------------------
+# CPU: the oracle's cluster step
+# --------------------------------------------------------------------------
+def test_oracle_bond_threshold():
+    assert O.lib().orc_bond_threshold(0.2) == 0 and O.lib().orc_bond_threshold(0.0) == 0
+    assert O.lib().orc_bond_threshold(-40.0) == 0xFFFFFFFF
+    p = 1.0 - math.exp(2.0 * KC)
+    assert O.lib().orc_bond_threshold(KC) == math.floor(p * 2**32)
+
+
+def test_oracle_cluster_limits():
+    """No open bond (K > 0): Wolff flips the seed alone, Swendsen-Wang every site on its
+    own coin.  Bonds open almost surely (K = -40) on a uniform lattice: one cluster."""
+    s = O.init_spins(16, 3)
+    for t in range(5):
+        _, f = O.cluster_update(s, 0.2, 9, 0, t, O.WOLFF)
+        assert f == [1]
+    _, f = O.cluster_update(s, 0.2, 9, 0, 0, O.SWENDSEN_WANG, n=20)
+    assert 0.4 * 256 < np.mean(f) < 0.6 * 256
+    up = np.ones((16, 16), dtype=np.int8)
+    s2, f = O.cluster_update(up, -40.0, 9, 0, 0, O.WOLFF, n=3)
+    assert f == [256, 256, 256] and np.array_equal(s2, -up)
+    _, f = O.cluster_update(up, -40.0, 9, 0, 0, O.SWENDSEN_WANG, n=8)
+    assert set(f) <= {0, 256} and len(set(f)) == 2
+
+
+def _oracle_wolff_means(L, K, seed, n_eq, n_steps):
+    s = O.init_spins(L, seed)
+    s, _ = O.cluster_update(s, K, seed, 0, 0, O.WOLFF, n=n_eq)
+    size = bonds = 0
+    for k in range(n_steps):
+        s, f = O.cluster_update(s, K, seed, 0, n_eq + k, O.WOLFF)
+        size += f[0]
+        bonds += bond_sum(s)
+    return size / n_steps, bonds / n_steps
+
+
+@pytest.mark.parametrize("a", [0, 1])
+def test_oracle_wolff_matches_reference(a):
+    """The oracle's Wolff step (the device's bond draws) and the reference's own step
+    (its breadth-first growth and random numbers) give the same mean cluster size and
+    bond sum at L = 8, 16 for K = Kc, -0.40, -0.50 (independent chains on both sides)."""
+    g = np.load(GOLDEN)
+    L = int(g["L"][a])
+    for b, K in enumerate(g["K"]):
+        ours = np.array([_oracle_wolff_means(L, float(K), 300 + 10 * b + k, 1000, 8000) for k in range(5)])
+        assert within(ours[:, 0], g["size"][a, b]), (L, K, ours[:, 0], g["size"][a, b])
+        assert within(ours[:, 1], g["bond"][a, b]), (L, K, ours[:, 1], g["bond"][a, b])
+
+
+# --------------------------------------------------------------------------
+# GPU: the device labelling against the oracle, bit for bit
+# --------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def M(mcrg_lib):
+    import mcrg_gb300
+    return mcrg_gb300
+
+
+def assert_moments_equal(a: MomentSums, b: MomentSums):
+    assert a.n_samples == b.n_samples
+    assert a.S == b.S
+    assert a.SbS == b.SbS
+    assert a.SbSb == b.SbSb
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["wolff", "sw"])
+@pytest.mark.parametrize("L", [4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048])
+def test_cluster_update_bit_exact(M, L, kind):
+    """Spins and flipped counts after cluster updates equal the oracle's: one-tile
+    lattices (L <= 32), tiles merged across edges (L >= 64), shared-memory and HBM
+    contexts (L >= 512), couplings with small, critical and percolating clusters and
+    none (K > 0)."""
+    Ks = (KC, -0.3, -0.7, 0.2) if L <= 256 else (KC, -0.7)  # HBM contexts: fast acceptance regime only
+    n = 4 if L <= 512 else 2
+    for q, K in enumerate(Ks):
+        seed, rep = 17 + L + q, 2
+        lat = M.Lattice(L, K, seed=seed, replica=rep)
+        lat.sweep(3)
+        s0 = lat.spins_
+        f = lat.cluster_update(n, kind)
+        want, flips = O.cluster_update(s0, K, seed, rep, 3, KIND[kind], n=n)
+        assert f == sum(flips), (L, K, f, flips)
+        np.testing.assert_array_equal(lat.spins_, want, err_msg="L=%d K=%g %s" % (L, K, kind))
+        assert lat.counters()[0] == 3 + n
+        lat.close()
+
+
+@pytest.mark.gpu
+def test_cluster_update_then_sweeps(M):
+    """Cluster updates and sweeps share one update counter: a sweep after two Wolff
+    updates draws at update index 2 on both sides."""
+    L, seed = 64, 5
+    lat = M.Lattice(L, KC, seed=seed)
+    s0 = lat.spins_
+    lat.cluster_update(2, "wolff")
+    lat.sweep(1)
+    s, _ = O.cluster_update(s0, KC, seed, 0, 0, O.WOLFF, n=2)
+    s = O.sweep(s, KC, seed, 0, 2, 1)
+    np.testing.assert_array_equal(lat.spins_, s)
+    lat.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,C,kind", [(4, 5, "wolff"), (8, 2, "wolff"), (16, 5, "sw"), (64, 2, "wolff"),
+                                      (256, 3, "sw"), (512, 2, "wolff")])
+def test_measure_cluster_bit_exact(M, L, C, kind):
+    """mcrg_measure_cluster: n_samples x (updates_between cluster updates + blocking and
+    coupling sums at every level) gives the oracle's moments, bin for bin."""
+    seed, rep, ns, ub = 77 + L, 3, 6, 2
+    nl = int(math.log2(L)) - 1
+    lat = M.Lattice(L, KC, seed=seed, replica=rep, n_couplings=C)
+    s = lat.spins_
+    tot, bins = lat.measure_cluster(ns, ub, kind, bin_size=4)
+    trace = np.zeros((ns, nl + 1, C), dtype=np.int64)
+    for q in range(ns):
+        s, _ = O.cluster_update(s, KC, seed, rep, q * ub, KIND[kind], n=ub)
+        trace[q] = O.measure(s, C, nl, seed, rep, q)
+    assert_moments_equal(tot, MomentSums.from_trace(trace))
+    assert len(bins) == 2
+    assert_moments_equal(bins[0], MomentSums.from_trace(trace[:4]))
+    assert_moments_equal(bins[1], MomentSums.from_trace(trace[4:]))
+    np.testing.assert_array_equal(lat.spins_, s)
+    assert lat.counters() == (ns * ub, ns)
+    lat.close()
+
+
+# --------------------------------------------------------------------------
+# GPU: the update rule against the reference and exact results
+# --------------------------------------------------------------------------
+@pytest.mark.gpu
+def test_device_wolff_matches_reference(M):
+    """Device Wolff chains at L = 16, 32 reproduce the reference's mean cluster size and
+    bond sum per step (independent chains on both sides, 5 standard errors)."""
+    g = np.load(GOLDEN)
+    for a in (1, 2):
+        L = int(g["L"][a])
+        for b, K in enumerate(g["K"]):
+            ours = []
+            for k in range(5):
+                lat = M.Lattice(L, float(K), seed=500 + 10 * b + k)
+                lat.cluster_update(1000, "wolff")
+                size = bonds = 0
+                n = 3000
+                for _ in range(n):
+                    size += lat.cluster_update(1, "wolff")
+                    bonds += bond_sum(lat.spins_)
+                ours.append((size / n, bonds / n))
+                lat.close()
+            ours = np.array(ours)
+            assert within(ours[:, 0], g["size"][a, b]), (L, K, ours[:, 0], g["size"][a, b])
+            assert within(ours[:, 1], g["bond"][a, b]), (L, K, ours[:, 1], g["bond"][a, b])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["wolff", "sw"])
+def test_cluster_chain_matches_exact_4x4(M, kind):
+    """The largest T-matrix eigenvalue of a cluster-update chain at L = 4, K = Kc against
+    exact enumeration of the 4x4 lattice."""
+    from mcrg_gb300.tmatrix import jackknife
+
+    lat = M.Lattice(4, KC, seed=4321)
+    lat.cluster_update(500, kind)
+    _, bins = lat.measure_cluster(100000, 1, kind, bin_size=5000)
+    est, err = jackknife(bins)
+    lam = O.exact4_lambda(KC, 2)
+    assert abs(est[0] - lam) < 5 * err[0] + 1e-3, (est, err, lam)
+    lat.close()
