@@ -11,14 +11,18 @@
 //   1. cl_tile_kernel: a CTA draws the bonds of a T x T tile (T = 32, or L
 //      below that), unites the sites of open in-tile bonds with a
 //      shared-memory union-find and writes every site's label: the smallest
-//      natural index i*L + j of its in-tile component;
+//      natural index i*L + j of its in-tile component.  With T = 32 a warp
+//      owns a tile row: the row's open horizontal bonds form a ballot mask,
+//      every site points at the first site of its run (count leading zeros),
+//      and only vertical bonds are united, one per pair of runs;
 //   2. cl_merge_kernel (L > 32): every open bond that crosses a tile edge
 //      unites the two trees of the global forest; atomicMin links the larger
 //      root under the smaller, so a root is always the smallest index of its
 //      tree and, at the end, of its cluster;
 //   3. cl_flip_kernel: every site finds its root; Wolff flips the sites that
 //      share the seed's root, Swendsen-Wang the sites whose root draws a set
-//      bit; the flips are counted.
+//      bit; the flips are counted.  With T = 32 a CTA loads its tile's labels
+//      and resolves the global root (and coin) once per in-tile component.
 // The result depends only on the bond draws, never on the order in which
 // threads unite, so it is reproducible and equal to the oracle's labelling.
 // Union and find loops make progress by construction (labels only decrease);
@@ -68,11 +72,28 @@ __device__ __forceinline__ int find_root(const int* par, int x, int* err) {
   return x;
 }
 
+// Root of x with path halving: each visited link is lowered to its
+// grandparent by atomicMin, so links still only decrease.
+__device__ __forceinline__ int find_halve(int* par, int x, int* err) {
+  const volatile int* vp = par;
+  for (int it = 0; it < kFindLimit; ++it) {
+    const int p = vp[x];
+    if (p == x) return x;
+    const int gp = vp[p];
+    if (gp == p) return p;
+    atomicMin(&par[x], gp);
+    x = gp;
+  }
+  atomicOr(err, 2);
+  return x;
+}
+
 // Unites the trees of a and b: the larger root is linked under the smaller.
+template <bool HALVE = false>
 __device__ __forceinline__ void unite(int* par, int a, int b, int* err) {
   for (int it = 0; it < kFindLimit; ++it) {
-    a = find_root(par, a, err);
-    b = find_root(par, b, err);
+    a = HALVE ? find_halve(par, a, err) : find_root(par, a, err);
+    b = HALVE ? find_halve(par, b, err) : find_root(par, b, err);
     if (a == b) return;
     if (a < b) {
       const int t = a;
@@ -121,6 +142,63 @@ __global__ void __launch_bounds__(256) cl_tile_kernel(const uint8_t* __restrict_
   }
 }
 
+// Tiles of 32 x 32 (L >= 32): warp w owns rows w, w+8, w+16, w+24.  Sites
+// point at the first site of their horizontal run; vertical bonds unite runs.
+__global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restrict__ st, int L,
+                                                        int* __restrict__ label, Key key, uint32_t rep, uint32_t t,
+                                                        uint32_t tb, int* err) {
+  __shared__ int par[1024];
+  __shared__ uint8_t sp[33 * 32];  // spins of the tile's rows and of the row below it
+  __shared__ uint32_t hb[32], vb[32];
+  const int tpr = L >> 5, ti = blockIdx.x / tpr, tj = blockIdx.x - ti * tpr;
+  const int i0 = ti << 5, j0 = tj << 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool one = L == 32;  // a one-tile lattice: its wrap bonds are in-tile bonds
+  if (threadIdx.x < 66) {  // 33 rows x 2 colours: 16 bytes each, de-interleaved into natural order
+    const int r = threadIdx.x >> 1, c = threadIdx.x & 1, i = (i0 + r) & (L - 1), h = L / 2;
+    const uint4 v = *reinterpret_cast<const uint4*>(st + (size_t)c * L * h + (size_t)i * h + (j0 >> 1));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    const int q = (i + c) & 1;  // column parity of colour c in row i (j0 is even)
+#pragma unroll
+    for (int b = 0; b < 16; ++b) sp[r * 32 + 2 * b + q] = (uint8_t)((w[b >> 2] >> (8 * (b & 3))) & 0xFFu);
+  }
+  __syncthreads();
+  for (int rp = warp; rp < 16; rp += 8) {  // row pairs 2rp, 2rp+1: lane l draws pair l & 15 of row 2rp + (l >> 4)
+    const uint4 R = stream_block(key, rep, P_BOND, 0u, (uint32_t)(i0 + 2 * rp + (lane >> 4)),
+                                 (uint32_t)((j0 >> 1) + (lane & 15)), t);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int r = 2 * rp + h, src = h * 16 + (lane >> 1);
+      const uint32_t wx = __shfl_sync(0xFFFFFFFFu, R.x, src), wy = __shfl_sync(0xFFFFFFFFu, R.y, src);
+      const uint32_t wz = __shfl_sync(0xFFFFFFFFu, R.z, src), ww = __shfl_sync(0xFFFFFFFFu, R.w, src);
+      const uint32_t ur = (lane & 1) ? wz : wx, ud = (lane & 1) ? ww : wy;
+      const uint32_t s = sp[r * 32 + lane];
+      const bool right = ur < tb && (lane < 31 || one) && sp[r * 32 + ((lane + 1) & 31)] == s;
+      const bool down = ud < tb && (r < 31 || one) && sp[(r + 1) * 32 + lane] == s;
+      const uint32_t hm = __ballot_sync(0xFFFFFFFFu, right), vm = __ballot_sync(0xFFFFFFFFu, down);
+      const uint32_t starts = ~(hm << 1);  // bit c: the bond (c-1, c) is closed (bit 0 always); the wrap bit drops out
+      const uint32_t low = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+      par[r * 32 + lane] = r * 32 + (31 - __clz(starts & low));
+      if (lane == 0) {
+        hb[r] = hm;
+        vb[r] = vm;
+      }
+    }
+  }
+  __syncthreads();
+  for (int r = warp; r < 32; r += 8) {
+    const int rn = (r + 1) & 31;
+    const uint32_t v = vb[r], hr = hb[r], hn = hb[rn];
+    const uint32_t dup = (v & hr & hn) << 1;  // column c-1 already joins the same two runs
+    if (((v & ~dup) >> lane) & 1u) unite<true>(par, r * 32 + lane, rn * 32 + lane, err);
+    if (one && lane == 31 && (hr >> 31)) unite<true>(par, r * 32 + 31, r * 32, err);  // horizontal wrap
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x < 1024; x += 256) {
+    const int r = find_root(par, x, err);
+    label[(size_t)(i0 + (x >> 5)) * L + j0 + (x & 31)] = (i0 + (r >> 5)) * L + j0 + (r & 31);
+  }
+}
+
 // Open bonds that cross a tile edge (L > kTile): the right bonds of column
 // T-1 and the down bonds of row T-1 of every tile (periodic wrap included).
 __global__ void __launch_bounds__(256) cl_merge_kernel(const uint8_t* __restrict__ st, int L, int* label, Key key,
@@ -142,6 +220,91 @@ __global__ void __launch_bounds__(256) cl_merge_kernel(const uint8_t* __restrict
       if (u < tb && nat_spin(st, L, i, j) == nat_spin(st, L, (i + 1) & m, j))
         unite(label, i * L + j, ((i + 1) & m) * L + j, err);
     }
+  }
+}
+
+// Every other bit of x (bits 0, 2, .., 30) packed into the low 16 bits.
+__device__ __forceinline__ uint32_t even_bits(uint32_t x) {
+  x &= 0x55555555u;
+  x = (x | (x >> 1)) & 0x33333333u;
+  x = (x | (x >> 2)) & 0x0F0F0F0Fu;
+  x = (x | (x >> 4)) & 0x00FF00FFu;
+  return (x | (x >> 8)) & 0x0000FFFFu;
+}
+
+// Flips of a 32 x 32 tile (L >= 32): the global root and the coin of every
+// in-tile component are resolved once, then every site looks them up; a
+// warp owns a tile row and applies its flips as two 16-byte XORs.
+__global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st, int L, int lg,
+                                                        const int* __restrict__ label, int kind, Key key, uint32_t rep,
+                                                        uint32_t t, unsigned long long* count, int* err) {
+  __shared__ int lbl[1024], groot[1024];
+  __shared__ uint8_t need[1024], coin[1024];
+  __shared__ int seed_root;
+  __shared__ unsigned long long warp_cnt[8];
+  const int tpr = L >> 5, ti = blockIdx.x >> (lg - 5), tj = blockIdx.x & (tpr - 1);
+  const int i0 = ti << 5, j0 = tj << 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool wolff = kind == MCRG_UPDATE_WOLFF;
+  if (wolff && threadIdx.x == 0) {
+    const uint4 r = stream_block(key, rep, P_CLUSTER, 0u, 0u, 0u, t);
+    seed_root = find_root(label, (int)(r.x & (uint32_t)(L * L - 1)), err);
+  }
+  for (int x = threadIdx.x; x < 1024; x += 256) need[x] = 0;
+  __syncthreads();
+  // the in-tile index of a label, or -1 when it lies outside the tile
+  auto loc = [&](int v) {
+    const int vi = (v >> lg) - i0, vj = (v & (L - 1)) - j0;
+    return ((unsigned)vi < 32u && (unsigned)vj < 32u) ? (vi << 5) + vj : -1;
+  };
+  for (int x = threadIdx.x; x < 1024; x += 256) {
+    const int v = label[((size_t)(i0 + (x >> 5)) << lg) + j0 + (x & 31)];
+    lbl[x] = v;
+    const int q = loc(v);
+    if (q >= 0) need[q] = 1;
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x < 1024; x += 256)
+    if (need[x]) {
+      const int r = find_root(label, ((i0 + (x >> 5)) << lg) + j0 + (x & 31), err);
+      groot[x] = r;
+      if (!wolff)
+        coin[x] = (uint8_t)(stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)r >> 16, (uint32_t)r & 0xFFFFu, t).x & 1u);
+    }
+  __syncthreads();
+  const int h = L / 2;
+  unsigned cnt = 0;
+  for (int r = warp; r < 32; r += 8) {
+    const int v = lbl[(r << 5) + lane], q = loc(v);
+    bool flip;
+    if (q >= 0) {
+      flip = wolff ? groot[q] == seed_root : coin[q] != 0;
+    } else {  // a tile root the merge linked elsewhere: its own root
+      const int g = find_root(label, v, err);
+      flip = wolff ? g == seed_root
+                   : (stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)g >> 16, (uint32_t)g & 0xFFFFu, t).x & 1u) != 0;
+    }
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, flip);
+    if (lane < 2 && m) {  // lane c: the 16 bytes of colour c in this row segment
+      const int i = i0 + r, c = lane, par = (i + c) & 1;  // colour c holds the columns of parity (i + c) & 1
+      const uint32_t bits = even_bits(m >> par);
+      if (bits) {
+        uint4* p = reinterpret_cast<uint4*>(st + (size_t)c * L * h + (size_t)i * h + (j0 >> 1));
+        uint4 v4 = *p;
+        v4.x ^= spread4(bits);
+        v4.y ^= spread4(bits >> 4);
+        v4.z ^= spread4(bits >> 8);
+        v4.w ^= spread4(bits >> 12);
+        *p = v4;
+      }
+    }
+    if (lane == 0) cnt += (unsigned)__popc(m);
+  }
+  if (lane == 0) warp_cnt[warp] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long tot = 0;
+    for (int w = 0; w < 8; ++w) tot += warp_cnt[w];
+    if (tot) atomicAdd(count, tot);
   }
 }
 
@@ -189,16 +352,23 @@ cudaError_t launch_cluster_update(uint8_t* d_state, int L, int* d_label, int kin
                                   uint32_t t, uint32_t bond_threshold, unsigned long long* d_count, int* d_err,
                                   int num_sms, cudaStream_t s) {
   const int T = L < kTile ? L : kTile, tiles = (L / T) * (L / T);
-  cl_tile_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
+  if (L >= kTile)
+    cl_tile32_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
+  else
+    cl_tile_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
   if (L > kTile) {
     const long long edges = 2LL * L * (L / kTile);
     long long blocks = (edges + 255) / 256;
     if (blocks > 8LL * num_sms) blocks = 8LL * num_sms;
     cl_merge_kernel<<<(int)blocks, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
   }
-  long long blocks = ((long long)L * L + 255) / 256;
-  if (blocks > 16LL * num_sms) blocks = 16LL * num_sms;
-  cl_flip_kernel<<<(int)blocks, 256, 0, s>>>(d_state, L, d_label, kind, key, replica, t, d_count, d_err);
+  if (L >= kTile) {
+    int lg = 0;
+    while ((1 << lg) < L) ++lg;
+    cl_flip32_kernel<<<tiles, 256, 0, s>>>(d_state, L, lg, d_label, kind, key, replica, t, d_count, d_err);
+  } else {
+    cl_flip_kernel<<<1, 256, 0, s>>>(d_state, L, d_label, kind, key, replica, t, d_count, d_err);
+  }
   return cudaGetLastError();
 }
 
