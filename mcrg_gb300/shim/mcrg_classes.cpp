@@ -106,6 +106,12 @@ long long nn_sum(const SpinMatrix& s) {
 
 }  // namespace
 
+// n Monte Carlo steps of the given rule on the context.
+static int advance(mcrg_ctx* ctx, Update u, int64_t n) {
+  if (u == Update::Metropolis) return mcrg_sweep(ctx, n);
+  return mcrg_cluster_update(ctx, n, u == Update::Wolff ? MCRG_UPDATE_WOLFF : MCRG_UPDATE_SWENDSEN_WANG, nullptr);
+}
+
 // src/ising.cpp:14-84.  The sweeps between two logged iterations run in one
 // device call (the chain is the same as sweeping one by one).  The logged
 // columns follow the reference's arithmetic with one process: E = K S_nn / N^2
@@ -114,7 +120,7 @@ long long nn_sum(const SpinMatrix& s) {
 // processes (zero here).
 void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool write) {
   if (!write) {
-    check(mcrg_sweep(p->ctx(), n_samples_eq), "mcrg_sweep");
+    check(advance(p->ctx(), update_, n_samples_eq), "equilibrate");
     p->refresh();
     return;
   }
@@ -132,7 +138,7 @@ void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool 
   try {
     for (int n = 1; n <= n_samples_eq; ++n) {
       if (!write_iter(n)) continue;
-      check(mcrg_sweep(p->ctx(), n - done), "mcrg_sweep");
+      check(advance(p->ctx(), update_, n - done), "equilibrate");
       done = n;
       p->sync_spins();
       const int NN = p->N_ * p->N_;
@@ -146,7 +152,7 @@ void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool 
       fprintf(f, "%i, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e\n", n, E / p->n_spins_, E_sigma / p->n_spins_, C,
               M / p->n_spins_, M_sigma / p->n_spins_, Chi);
     }
-    if (done < n_samples_eq) check(mcrg_sweep(p->ctx(), n_samples_eq - done), "mcrg_sweep");
+    if (done < n_samples_eq) check(advance(p->ctx(), update_, n_samples_eq - done), "equilibrate");
   } catch (...) {
     fclose(f);
     throw;
@@ -163,7 +169,7 @@ void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool 
 }
 
 void IsingModel::sample_new_configuration(std::shared_ptr<Lattice> p) {
-  check(mcrg_sweep(p->ctx(), 1), "mcrg_sweep");
+  check(advance(p->ctx(), update_, 1), "sample_new_configuration");
   p->refresh();
 }
 
@@ -207,9 +213,16 @@ void MonteCarloRenormalizationGroup::calc_critical_exponent(int n_samples_eq, in
   mcrg_ctx* ctx = nullptr;
   check(mcrg_alloc(&ctx, &cfg), "mcrg_alloc");
   mcrg_moments mom;
-  int rc = mcrg_sweep(ctx, n_samples_eq);
+  int rc = advance(ctx, update_, n_samples_eq);
   printf("Sampling %i configurations...\n", n_samples);
-  if (rc == MCRG_OK) rc = mcrg_measure(ctx, n_samples, 1, &mom, 0, nullptr, 0);
+  if (rc == MCRG_OK) {
+    if (update_ == Update::Metropolis)
+      rc = mcrg_measure(ctx, n_samples, 1, &mom, 0, nullptr, 0);
+    else
+      rc = mcrg_measure_cluster(ctx, n_samples, 1,
+                                update_ == Update::Wolff ? MCRG_UPDATE_WOLFF : MCRG_UPDATE_SWENDSEN_WANG, &mom, 0,
+                                nullptr, 0);
+  }
   mcrg_free(ctx);
   if (rc != MCRG_OK) {
     if (f) fclose(f);

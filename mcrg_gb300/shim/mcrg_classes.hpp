@@ -8,8 +8,11 @@
 // caller can observe:
 //   - the lattice lives on the GPU; spins_ is a host mirror refreshed after
 //     every device operation (set mirror_spins_ = false to skip the copy);
-//   - sample_new_configuration() is one checkerboard Metropolis sweep, not a
-//     Wolff cluster step (same stationary distribution);
+//   - sample_new_configuration() is one checkerboard Metropolis sweep by
+//     default (same stationary distribution as the reference's Wolff step);
+//     update_ = Update::Wolff makes it the reference's own rule, one Wolff
+//     cluster grown and flipped on the device (Update::SwendsenWang: every
+//     cluster flipped with probability 1/2);
 //   - the RG eigen-solve is a small FP64 routine (tmatrix.hpp) instead of
 //     Eigen, applied to exact integer moment sums;
 //   - errors from the device surface as McrgError exceptions on the C++ side
@@ -91,10 +94,16 @@ class Lattice {
   mcrg_ctx* ctx_ = nullptr;
 };
 
+// Update rule of a Monte Carlo step: a checkerboard Metropolis sweep, or a
+// cluster update on the device (mcrg_cluster_update).
+enum class Update { Metropolis, Wolff, SwendsenWang };
+
 class IsingModel {
  public:
   explicit IsingModel(double K);
   ~IsingModel() {}
+
+  Update update_ = Update::Metropolis;
 
   void equilibrate(std::shared_ptr<Lattice> pLattice, int n_samples_eq, bool write);
   void sample_new_configuration(std::shared_ptr<Lattice> pLattice);
@@ -112,8 +121,10 @@ class MonteCarloRenormalizationGroup {
 
   int b_;
 
-  // src/mcrg.cpp:22-144: prints and writes critical_exponent_N_<N>_K_<K>.txt
+  // src/mcrg.cpp:22-144: prints and writes critical_exponent_N_<N>_K_<K>.txt;
+  // equilibration and the step between samples use update_
   void calc_critical_exponent(int n_samples_eq, int n_samples, int N, double K);
+  Update update_ = Update::Metropolis;
 
   // src/mcrg.cpp:145-189: iterated flow matching of lattices of side L and
   // L/b; prints, writes critical_point_L_<L>_K_<K0>.txt, returns the last Kc

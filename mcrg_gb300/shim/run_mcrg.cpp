@@ -1,6 +1,6 @@
 // run_mcrg -- the reference's src/main.cpp call sequence against the
 // GB300 library: MonteCarloRenormalizationGroup(b).calc_critical_exponent.
-// Usage: run_mcrg N n_eq n_samples K [seed] [n_couplings]
+// Usage: run_mcrg N n_eq n_samples K [seed] [n_couplings] [metropolis|wolff|sw]
 //        run_mcrg locate L n_iterations n_eq n_samples K0 [seed]
 //          (MonteCarloRenormalizationGroup::locate_critical_point)
 //        run_mcrg rgnn N seed W00 W01 W10 W11  (Lattice::rgnn_scalar_output of the initial coin)
@@ -66,6 +66,10 @@ int main(int argc, char** argv) {
     MonteCarloRenormalizationGroup MCRG(2);
     if (argc > 5) MCRG.seed_ = strtoull(argv[5], nullptr, 10);
     if (argc > 6) MCRG.n_couplings_ = atoi(argv[6]);
+    if (argc > 7) {  // update rule: metropolis (default), wolff, sw
+      const std::string u = argv[7];
+      MCRG.update_ = u == "wolff" ? Update::Wolff : (u == "sw" ? Update::SwendsenWang : Update::Metropolis);
+    }
     MCRG.calc_critical_exponent(n_eq, n_samples, N, K);
     for (size_t n = 0; n < MCRG.lambdas_.size(); ++n) printf("LAMBDA %zu %.12f\n", n, MCRG.lambdas_[n]);
   } catch (const McrgError& e) {

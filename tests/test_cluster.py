@@ -196,3 +196,24 @@ def test_cluster_chain_matches_exact_4x4(M, kind):
     lam = O.exact4_lambda(KC, 2)
     assert abs(est[0] - lam) < 5 * err[0] + 1e-3, (est, err, lam)
     lat.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule", ["wolff", "sw"])
+def test_cpp_calc_critical_exponent_with_cluster_updates(M, rule):
+    """run_mcrg with update rule wolff / sw (MonteCarloRenormalizationGroup::update_, the
+    C++ drop-in for src/main.cpp) gives the eigenvalues of the same cluster chain run
+    through the Python binding."""
+    import subprocess
+    from mcrg_gb300 import build as B
+    from mcrg_gb300.tmatrix import eigenvalues
+
+    exe = B.build_shim()
+    r = subprocess.run([exe, "16", "200", "2000", repr(KC), "5", "2", rule], capture_output=True, text=True,
+                       cwd=os.path.dirname(exe), check=True)
+    lam = [float(l.split()[2]) for l in r.stdout.splitlines() if l.startswith("LAMBDA")]
+    lat = M.Lattice(16, KC, seed=5, n_couplings=2)
+    lat.cluster_update(200, rule)
+    tot, _ = lat.measure_cluster(2000, 1, rule)
+    lat.close()
+    np.testing.assert_allclose(lam, eigenvalues(tot), rtol=1e-9, atol=1e-12)
