@@ -263,7 +263,10 @@ typedef struct {
   int32_t L;
   int32_t n_levels;    /* < 0: log2(L)-1 */
   int32_t n_couplings;
-  int32_t flags;       /* reserved, 0 */
+  int32_t flags;       /* update rule: 0 = checkerboard sweeps, MCRG_UPDATE_WOLFF or
+                          MCRG_UPDATE_SWENDSEN_WANG = cluster updates (n_eq and sweeps_between
+                          then count cluster updates); cluster requests up to L = 256 run as
+                          resident chains */
   double K;
   uint64_t seed;
   uint32_t replica;

@@ -299,8 +299,12 @@ def _cluster_kind(kind) -> int:
 
 
 def make_request(L: int, K: float, seed: int, replica: int = 0, n_eq: int = 0, n_samples: int = 0,
-                 sweeps_between: int = 1, n_levels: int = -1, n_couplings: int = 2) -> _abi.Request:
-    return _abi.Request(L, n_levels, n_couplings, 0, float(K), seed, replica, 0, n_eq, n_samples, sweeps_between)
+                 sweeps_between: int = 1, n_levels: int = -1, n_couplings: int = 2,
+                 update: str = "metropolis") -> _abi.Request:
+    """One batched / served solve.  update: "metropolis" (checkerboard sweeps), "wolff" or
+    "sw" (cluster updates; n_eq and sweeps_between then count cluster updates)."""
+    flags = 0 if update in ("metropolis", 0) else _cluster_kind(update)
+    return _abi.Request(L, n_levels, n_couplings, flags, float(K), seed, replica, 0, n_eq, n_samples, sweeps_between)
 
 
 def batch_run(requests, device: int = 0, use_graph: bool = True, raw: bool = False):

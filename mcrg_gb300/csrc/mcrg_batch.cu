@@ -76,6 +76,7 @@ int check_request(const mcrg_request* r) {
   if (r->n_couplings < 1 || r->n_couplings > MCRG_MAX_COUPLINGS) return MCRG_EINVAL;
   if (r->n_eq < 0 || r->n_samples < 0 || r->sweeps_between < 0) return MCRG_EINVAL;
   if (!(r->K == r->K)) return MCRG_EINVAL;
+  if (r->flags != 0 && r->flags != MCRG_UPDATE_WOLFF && r->flags != MCRG_UPDATE_SWENDSEN_WANG) return MCRG_EINVAL;
   const int mx = ilog2i(r->L) - 1;
   const int nl = r->n_levels < 0 ? mx : r->n_levels;
   if (nl > mx) return MCRG_EINVAL;
@@ -83,6 +84,15 @@ int check_request(const mcrg_request* r) {
 }
 
 int64_t n_dev_bins(const mcrg_request* r) { return r->n_samples > 0 ? (r->n_samples + kBatchBin - 1) / kBatchBin : 0; }
+
+// Whether a request runs as a shared-memory-resident chain: sweeps in the
+// fast acceptance regime up to MCRG_RESIDENT_MAX_L, cluster updates while
+// labels, levels and moments fit one CTA (L <= 256).
+bool runs_resident(const mcrg_request* r, int nl) {
+  const bool fast = make_accept(r->K).fast;
+  if (r->flags) return cluster_resident(r->L, nl, MCRG_MAX_COUPLINGS, fast);
+  return r->L <= MCRG_RESIDENT_MAX_L && fast;
+}
 
 void fill_job(ChainJob* j, const mcrg_request* r, int nl, uint8_t* state, mcrg_moments* bins) {
   memset(j, 0, sizeof *j);
@@ -98,6 +108,8 @@ void fill_job(ChainJob* j, const mcrg_request* r, int nl, uint8_t* state, mcrg_m
   j->n_samples = r->n_samples;
   j->sweeps_between = r->sweeps_between;
   j->bin_size = kBatchBin;
+  j->update = r->flags;
+  j->bond_tb = r->flags ? bond_threshold(r->K) : 0u;
   j->state = state;
   j->bins = bins;
   j->acc = make_accept(r->K);
@@ -118,8 +130,13 @@ int run_tiled_request(const mcrg_request* r, int device, mcrg_moments* out) {
   mcrg_ctx* c = nullptr;
   int rc = mcrg_alloc(&c, &cfg);
   if (rc) return rc;
-  rc = mcrg_sweep(c, r->n_eq);
-  if (!rc) rc = mcrg_measure(c, r->n_samples, r->sweeps_between, out, 0, nullptr, 0);
+  if (r->flags) {
+    rc = mcrg_cluster_update(c, r->n_eq, r->flags, nullptr);
+    if (!rc) rc = mcrg_measure_cluster(c, r->n_samples, r->sweeps_between, r->flags, out, 0, nullptr, 0);
+  } else {
+    rc = mcrg_sweep(c, r->n_eq);
+    if (!rc) rc = mcrg_measure(c, r->n_samples, r->sweeps_between, out, 0, nullptr, 0);
+  }
   mcrg_free(c);
   return rc;
 }
@@ -204,8 +221,8 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     nl[i] = check_request(&reqs[i]);
     results[i].status = nl[i] < 0 ? nl[i] : MCRG_OK;
   }
-  // group resident requests by side
-  std::map<int, std::vector<int>> groups;
+  // group resident requests by side and chain form (bit planes, cluster updates)
+  std::map<std::pair<int, int>, std::vector<int>> groups;
   std::vector<int> tiled;
   size_t state_bytes = 0;
   int64_t total_bins = 0;
@@ -213,8 +230,9 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
   std::vector<int64_t> bin_off(n, 0);
   for (int i = 0; i < n; ++i) {
     if (results[i].status) continue;
-    if (reqs[i].L <= MCRG_RESIDENT_MAX_L && make_accept(reqs[i].K).fast) {
-      groups[reqs[i].L].push_back(i);
+    if (runs_resident(&reqs[i], nl[i])) {
+      const int mode = (make_accept(reqs[i].K).fast && reqs[i].L >= 64 ? 1 : 0) | (reqs[i].flags ? 2 : 0);
+      groups[{reqs[i].L, mode}].push_back(i);
       state_off[i] = state_bytes;
       state_bytes += (size_t)reqs[i].L * reqs[i].L;
       bin_off[i] = total_bins;
@@ -228,6 +246,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     BatchWorkspace& w = workspace(device);
     std::lock_guard<std::mutex> lk(w.mu);
     std::vector<std::pair<int, int>> ranges;  // (first job, count) per group
+    std::vector<int> modes;                   // chain form per group
     std::vector<int> order;                   // job index -> request index
     const size_t n_jobs = (size_t)n - tiled.size() - (size_t)std::count_if(results, results + n, [](const mcrg_result& r) {
                             return r.status != MCRG_OK;
@@ -239,6 +258,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
       size_t k = 0;
       for (auto it = groups.rbegin(); it != groups.rend(); ++it) {
         ranges.push_back({(int)k, (int)it->second.size()});
+        modes.push_back(it->first.second);
         for (int i : it->second) {
           fill_job(&w.h_jobs[k++], &reqs[i], nl[i], w.d_state + state_off[i], w.d_bins + bin_off[i]);
           order.push_back(i);
@@ -258,7 +278,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         int maxlev = 0;
         for (int q = 0; q < ranges[g].second; ++q) maxlev = std::max(maxlev, w.h_jobs[(size_t)ranges[g].first + q].n_levels);
         if (launch_chain(w.d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads,
-                         j0.L >= 64, sg) != cudaSuccess)  // every job of a group is in the fast regime
+                         (modes[g] & 1) != 0, sg, (modes[g] & 2) != 0) != cudaSuccess)
           rc = MCRG_EIO;
         cudaEventRecord(w.ev[g % kMaxGroups], sg);
         cudaStreamWaitEvent(s0, w.ev[g % kMaxGroups], 0);
@@ -424,8 +444,13 @@ void hbm_worker(mcrg_server* s) {
         rc = mcrg_alloc(&c, &cfg);
         if (!rc) cache[key] = c;
       }
-      if (!rc) rc = mcrg_sweep(c, r.n_eq);
-      if (!rc) rc = mcrg_measure(c, r.n_samples, r.sweeps_between, &res.moments, 0, nullptr, 0);
+      if (r.flags) {
+        if (!rc) rc = mcrg_cluster_update(c, r.n_eq, r.flags, nullptr);
+        if (!rc) rc = mcrg_measure_cluster(c, r.n_samples, r.sweeps_between, r.flags, &res.moments, 0, nullptr, 0);
+      } else {
+        if (!rc) rc = mcrg_sweep(c, r.n_eq);
+        if (!rc) rc = mcrg_measure(c, r.n_samples, r.sweeps_between, &res.moments, 0, nullptr, 0);
+      }
       res.status = rc;
     } else {  // outside the fast acceptance regime: a one-off context
       res.status = run_tiled_request(&r, s->cfg.device, &res.moments);
@@ -488,7 +513,7 @@ void server_loop(mcrg_server* s) {
       sl.nl = q.nl;
       sl.submit_s = q.submit_s;
       sl.nb = n_dev_bins(&q.r);
-      sl.tiled = !(q.r.L <= MCRG_RESIDENT_MAX_L && make_accept(q.r.K).fast);
+      sl.tiled = !runs_resident(&q.r, q.nl);
       if (sl.tiled) continue;  // handed to the HBM workers below
       uint8_t* base = s->arena + sl.off;
       ChainJob* d_job = reinterpret_cast<ChainJob*>(base);
@@ -503,7 +528,7 @@ void server_loop(mcrg_server* s) {
       }
       cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, sl.stream);
       cudaMemsetAsync(d_bins, 0, sizeof(mcrg_moments) * (size_t)(sl.nb > 0 ? sl.nb : 1), sl.stream);
-      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, j.L >= 64, sl.stream);  // fast regime
+      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, j.acc.fast && j.L >= 64, sl.stream, j.update != 0);
       if (sl.nb > 0)
         cudaMemcpyAsync(sl.h_bins, d_bins, sizeof(mcrg_moments) * (size_t)sl.nb, cudaMemcpyDeviceToHost, sl.stream);
       cudaEventRecord(sl.done, sl.stream);

@@ -134,7 +134,7 @@ int ensure_bins(mcrg_ctx* c, int64_t n) {
 
 // Runs one resident chain job for the context and returns the device bins.
 int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_between, int64_t bin_size,
-                 int64_t* n_bins_out, bool flow = false) {
+                 int64_t* n_bins_out, bool flow = false, int update = 0) {
   ChainJob j;
   memset(&j, 0, sizeof j);
   j.L = c->cfg.L;
@@ -154,6 +154,8 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   j.state = c->d_state;
   j.acc = c->acc;
   j.flow = flow ? 1 : 0;
+  j.update = update;
+  j.bond_tb = update ? bond_threshold(c->cfg.K) : 0u;
   int64_t nb = n_samples > 0 ? (n_samples + bin_size - 1) / bin_size : 0;
   if (nb > 0) {
     int rc = ensure_bins(c, nb);
@@ -162,7 +164,7 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   }
   j.bins = c->d_bins;
   CK(cudaMemcpyAsync(c->d_job, &j, sizeof j, cudaMemcpyHostToDevice, c->stream));
-  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.C, j.threads, j.acc.fast && j.L >= 64, c->stream));
+  CK(launch_chain(c->d_job, 1, j.L, j.n_levels, j.C, j.threads, j.acc.fast && j.L >= 64, c->stream, update != 0));
   c->t += (uint64_t)(n_eq + n_samples * sweeps_between);
   c->n += (uint64_t)n_samples;
   *n_bins_out = nb;
@@ -336,8 +338,10 @@ int mcrg_sweep(mcrg_ctx* c, int64_t n_sweeps) {
 
 // Sample loop shared by mcrg_measure (T-matrix moments) and
 // mcrg_measure_flow (flow moments, flow = true).
+// update: 0 = sweeps between samples; a cluster kind runs the whole loop in
+// the resident chain (shared-memory contexts only).
 static int measure_impl(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_moments* total,
-                        int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap, bool flow) {
+                        int64_t bin_size, mcrg_moments* bins, int64_t n_bins_cap, bool flow, int update = 0) {
   if (!c || n_samples < 0 || sweeps_between < 0) return MCRG_EINVAL;
   if (bins && (bin_size <= 0 || bin_size > kMaxDeviceBin || n_bins_cap < 0)) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
@@ -367,7 +371,7 @@ static int measure_impl(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, 
     CK(cudaMemcpyAsync(h.data(), tiled_bins(&c->tiled), sizeof(mcrg_moments) * (size_t)nb,
                        cudaMemcpyDeviceToHost, c->stream));
   } else {
-    int rc = run_resident(c, 0, n_samples, sweeps_between, dev_bin, &nb, flow);
+    int rc = run_resident(c, 0, n_samples, sweeps_between, dev_bin, &nb, flow, update);
     if (rc) return rc;
     h.resize((size_t)nb);
     CK(cudaMemcpyAsync(h.data(), c->d_bins, sizeof(mcrg_moments) * (size_t)nb, cudaMemcpyDeviceToHost,
@@ -440,6 +444,9 @@ int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between
   if (bins && (bin_size <= 0 || n_bins_cap < 0)) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
   const int nl = c->n_levels, C = c->cfg.n_couplings;
+  // shared-memory contexts: the whole loop in one resident chain launch
+  if (!c->is_tiled && cluster_resident(c->cfg.L, nl, C, c->acc.fast) && (!bins || bin_size <= kMaxDeviceBin))
+    return measure_impl(c, n_samples, updates_between, total, bin_size, bins, n_bins_cap, false, kind);
   if (total) {
     memset(total, 0, sizeof *total);
     total->n_levels = nl;

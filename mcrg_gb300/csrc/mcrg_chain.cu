@@ -23,6 +23,7 @@
 // resolving them in place.
 #include "mcrg_ops.cuh"
 #include "mcrg_resident_bits.cuh"
+#include "mcrg_resident_cluster.cuh"
 
 namespace mcrg {
 
@@ -56,7 +57,8 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
   const Accept acc = J.acc;
   // L >= 64 in the fast regime: levels of side >= 64 are plane words
   const bool bits = acc.fast && L >= 64;
-  const SmemPlan plan = make_plan(L, nl, C, bits);
+  const int upd = J.update;  // 0: sweeps, else the cluster update kind
+  const SmemPlan plan = make_plan(L, nl, C, bits, upd != 0);
   uint8_t* lat = smem;
   int* S = reinterpret_cast<int*>(smem + plan.s_off);
   int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
@@ -108,16 +110,22 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
   if (bits && tid < 2) qn[tid] = 0;
   __syncthreads();
 
-  uint32_t t = J.t0;
-  for (int64_t s = 0; s < J.n_eq; ++s) {
-    if (bits) resident::sweep(pl, L, t++, key, rep, acc, tid, T, oq, qn);
-    else chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
-  }
-  for (int64_t n = 0; n < J.n_samples; ++n) {
-    for (int64_t s = 0; s < J.sweeps_between; ++s) {
-      if (bits) resident::sweep(pl, L, t++, key, rep, acc, tid, T, oq, qn);
-      else chain_sweep(lat, L, t++, key, rep, acc, vec, tid, T, scratch);
+  // one Monte Carlo step at update index tt: a sweep, or a cluster update
+  auto step = [&](uint32_t tt) {
+    if (upd) {
+      uint8_t* work = smem + plan.cl_off;
+      if (bits) rcluster::update_planes(pl, L, work, key, rep, tt, J.bond_tb, upd, tid, T);
+      else rcluster::update_bytes(lat, L, work, key, rep, tt, J.bond_tb, upd, tid, T);
+    } else if (bits) {
+      resident::sweep(pl, L, tt, key, rep, acc, tid, T, oq, qn);
+    } else {
+      chain_sweep(lat, L, tt, key, rep, acc, vec, tid, T, scratch);
     }
+  };
+  uint32_t t = J.t0;
+  for (int64_t s = 0; s < J.n_eq; ++s) step(t++);
+  for (int64_t n = 0; n < J.n_samples; ++n) {
+    for (int64_t s = 0; s < J.sweeps_between; ++s) step(t++);
     // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
@@ -214,8 +222,9 @@ __global__ void couplings_once_kernel(const uint8_t* in, int N, int C, int* out)
 }
 
 cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
-                         cudaStream_t stream) {
-  const SmemPlan plan = make_plan(L, n_levels, C, planes);
+                         cudaStream_t stream, bool cluster) {
+  if (cluster && L > kClusterMaxL) return cudaErrorInvalidValue;
+  const SmemPlan plan = make_plan(L, n_levels, C, planes, cluster);
   constexpr int kMaxSmem = 227 * 1024;  // opt-in shared memory per CTA
   if (plan.bytes > kMaxSmem || threads > 512) return cudaErrorInvalidValue;
   const bool wide = threads > 256;

@@ -34,7 +34,6 @@
 namespace mcrg {
 namespace {
 
-constexpr uint32_t P_BOND = 5, P_CLUSTER = 6;
 constexpr int kTile = 32;
 constexpr int kFindLimit = 1 << 28;  // > L^2 for every supported L
 

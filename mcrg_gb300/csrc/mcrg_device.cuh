@@ -18,7 +18,7 @@ namespace mcrg {
 // Philox4x32-10 stream layout (mirrored by the oracle):
 //   key = (seed lo32, seed hi32)
 //   ctr = (row, purpose << 28 | sub << 20 | group, time, replica)
-enum : uint32_t { P_INIT = 1, P_SWEEP_HI = 2, P_SWEEP_LO = 3, P_TIE = 4 };
+enum : uint32_t { P_INIT = 1, P_SWEEP_HI = 2, P_SWEEP_LO = 3, P_TIE = 4, P_BOND = 5, P_CLUSTER = 6 };
 
 struct Key {
   uint32_t k0, k1;

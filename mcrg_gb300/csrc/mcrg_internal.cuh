@@ -23,7 +23,9 @@ struct ChainJob {
   mcrg_moments* bins; // ceil(n_samples / bin_size) outputs, zeroed by the host
   Accept acc;
   int32_t flow;       // 1: flow moments (sum S_l and S_l * S_0 of coupling 0) instead of the T-matrix moments
-  int32_t pad;
+  int32_t update;     // 0: checkerboard sweeps; MCRG_UPDATE_WOLFF / MCRG_UPDATE_SWENDSEN_WANG: cluster updates (L <= 256)
+  uint32_t bond_tb;   // cluster updates: floor((1 - exp(2K)) 2^32)
+  uint32_t pad;
 };
 
 // Shared-memory plan of a resident lattice, its blocked levels and (when
@@ -40,8 +42,12 @@ struct SmemPlan {
   int Ecap;     // entries the table holds (also fits the 2 (n_levels + 1) flow moments)
   int qn_off;   // planes: int qn[2] (padded to 16 bytes)
   int q_off;    // planes: uint4 queue entries (resident queue_cap(L))
+  int cl_off;   // cluster updates: labels, coins and the seed's root (mcrg_resident_cluster.cuh)
   int bytes;
 };
+
+// Largest side of a chain with resident cluster updates (16-bit site labels).
+constexpr int kClusterMaxL = 256;
 
 // Largest side of a resident chain: bytes up to MCRG_SMEM_MAX_L, bit planes
 // (fast acceptance regime) up to MCRG_RESIDENT_MAX_L.
@@ -49,7 +55,7 @@ __host__ __device__ inline bool resident_fits(int L, bool fast) {
   return L <= (fast ? MCRG_RESIDENT_MAX_L : MCRG_SMEM_MAX_L);
 }
 
-__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bool planes = false) {
+__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bool planes = false, bool cluster = false) {
   SmemPlan p;
   int off = 0, n = L;
   for (int l = 0; l <= n_levels; ++l, n >>= 1) {
@@ -75,20 +81,31 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bo
     const int q = L * L / 256;
     off += (q < 32 ? 32 : (q > 2048 ? 2048 : q)) * 16;  // resident::queue_cap(L)
   }
+  p.cl_off = -1;
+  if (cluster) {  // rcluster::work_bytes(L)
+    off = (off + 15) / 16 * 16;
+    p.cl_off = off;
+    off += ((L * L * 2 + 15) / 16) * 16 + ((L * L / 8 + 15) / 16) * 16 + 16;
+  }
   p.bytes = (off + 15) / 16 * 16;
   return p;
 }
 
 inline int moment_entries(int n_levels, int C) { return (n_levels + 1) * C + 2 * n_levels * C * C; }
 
+// Whether a chain with cluster updates fits one CTA's shared memory (227 KB).
+inline bool cluster_resident(int L, int n_levels, int C, bool fast) {
+  return L <= kClusterMaxL && make_plan(L, n_levels, C, fast && L >= 64, true).bytes <= 227 * 1024;
+}
+
 // Host: acceptance parameters for coupling K (FP64, see include/mcrg.h).
 Accept make_accept(double K);
 
 // Launch `n_jobs` chains (all with the same L, threads and acceptance regime:
 // `planes` = acc.fast && L >= 64; n_levels and C bound the shared memory of
-// every job).
+// every job; `cluster`: the jobs use cluster updates, L <= kClusterMaxL).
 cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
-                         cudaStream_t stream);
+                         cudaStream_t stream, bool cluster = false);
 
 // Stateless helpers on a device lattice in split layout (used by
 // mcrg_block_lattice / mcrg_lattice_couplings and the HBM path's tail).

@@ -132,19 +132,23 @@ def test_cluster_update_then_sweeps(M):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,C,kind", [(4, 5, "wolff"), (8, 2, "wolff"), (16, 5, "sw"), (64, 2, "wolff"),
-                                      (256, 3, "sw"), (512, 2, "wolff")])
-def test_measure_cluster_bit_exact(M, L, C, kind):
+@pytest.mark.parametrize("L,C,kind,K", [(4, 5, "wolff", KC), (8, 2, "wolff", KC), (16, 5, "sw", KC),
+                                        (16, 2, "wolff", -0.1), (64, 2, "wolff", KC), (128, 2, "sw", -0.1),
+                                        (256, 3, "sw", KC), (256, 2, "wolff", -0.1), (512, 2, "wolff", KC)])
+def test_measure_cluster_bit_exact(M, L, C, kind, K):
     """mcrg_measure_cluster: n_samples x (updates_between cluster updates + blocking and
-    coupling sums at every level) gives the oracle's moments, bin for bin."""
+    coupling sums at every level) gives the oracle's moments, bin for bin.  Shared-memory
+    contexts run the whole loop in one resident chain (byte levels, or bit planes in the
+    fast regime, L >= 64); a byte chain of L = 256 does not fit one CTA with its labels and
+    HBM contexts (L = 512) take the per-sample loop of device-wide updates."""
     seed, rep, ns, ub = 77 + L, 3, 6, 2
     nl = int(math.log2(L)) - 1
-    lat = M.Lattice(L, KC, seed=seed, replica=rep, n_couplings=C)
+    lat = M.Lattice(L, K, seed=seed, replica=rep, n_couplings=C)
     s = lat.spins_
     tot, bins = lat.measure_cluster(ns, ub, kind, bin_size=4)
     trace = np.zeros((ns, nl + 1, C), dtype=np.int64)
     for q in range(ns):
-        s, _ = O.cluster_update(s, KC, seed, rep, q * ub, KIND[kind], n=ub)
+        s, _ = O.cluster_update(s, K, seed, rep, q * ub, KIND[kind], n=ub)
         trace[q] = O.measure(s, C, nl, seed, rep, q)
     assert_moments_equal(tot, MomentSums.from_trace(trace))
     assert len(bins) == 2
@@ -217,3 +221,54 @@ def test_cpp_calc_critical_exponent_with_cluster_updates(M, rule):
     tot, _ = lat.measure_cluster(2000, 1, rule)
     lat.close()
     np.testing.assert_allclose(lam, eigenvalues(tot), rtol=1e-9, atol=1e-12)
+
+
+def _solo(M, r, kind):
+    lat = M.Lattice(r.L, r.K, seed=r.seed, replica=r.replica, n_couplings=r.n_couplings, n_levels=r.n_levels)
+    if kind == "metropolis":
+        lat.sweep(r.n_eq)
+        tot, _ = lat.measure(r.n_samples, r.sweeps_between)
+    else:
+        lat.cluster_update(r.n_eq, kind)
+        tot, _ = lat.measure_cluster(r.n_samples, r.sweeps_between, kind)
+    lat.close()
+    return tot
+
+
+def _cluster_mix(M):
+    rng = np.random.default_rng(9)
+    out = []
+    for i in range(18):
+        kind = ("metropolis", "wolff", "sw")[i % 3]
+        L = int(rng.choice([8, 16, 64, 128, 256, 512]))
+        K = -0.1 if i in (4, 10) else float(rng.uniform(-0.49, -0.43))
+        if L == 512:
+            K = KC  # HBM contexts: fast acceptance regime only
+        r = M.make_request(L, K, seed=40 + i, replica=i, n_eq=int(rng.integers(0, 4)),
+                           n_samples=int(rng.integers(1, 5)), sweeps_between=int(rng.integers(1, 3)),
+                           n_couplings=int(rng.choice([2, 5])), update=kind)
+        out.append((r, kind))
+    return out
+
+
+@pytest.mark.gpu
+def test_batch_and_server_cluster_requests(M):
+    """Batched and served requests with the reference's update rule (flags = Wolff /
+    Swendsen-Wang) next to sweep requests: every result equals the single-context chain of
+    the same request (resident cluster chains up to L = 256, device-wide updates above)."""
+    mix = _cluster_mix(M)
+    reqs = [r for r, _ in mix]
+    res = M.batch_run(reqs)
+    want = [_solo(M, r, kind) for r, kind in mix]
+    for (r, kind), (st, mom), w in zip(mix, res, want):
+        assert st == 0, (r.L, kind, st)
+        assert_moments_equal(mom, w)
+    srv = M.Server(slots=6, hbm_budget_bytes=1 << 30)
+    try:
+        tickets = [srv.submit(r) for r in reqs]
+        out = [srv.wait(t, 300) for t in tickets]
+        for (r, kind), o, w in zip(mix, out, want):
+            assert o.status == 0, (r.L, kind, o.status)
+            assert_moments_equal(M.moments_from_c(o.moments), w)
+    finally:
+        srv.close()
