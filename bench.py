@@ -249,15 +249,17 @@ def run_large(args, D: Dist) -> dict:
     }
 
 
-def batched_requests(M, n, sweeps, rank=0, seed0=1):
+def batched_requests(M, n, sweeps, rank=0, seed0=1, update="metropolis"):
     """The batched config: L ~ {16:.3, 32:.3, 64:.2, 128:.15, 256:.05}, K on a
-    33-point grid over [-0.49, -0.43], log2(L)-1 levels, measured every sweep."""
+    33-point grid over [-0.49, -0.43], log2(L)-1 levels, measured every sweep
+    (or every cluster update when update is "wolff" / "sw")."""
     import numpy as np
     rng = np.random.default_rng(7 + rank)
     Ls = rng.choice([16, 32, 64, 128, 256], size=n, p=[0.3, 0.3, 0.2, 0.15, 0.05])
     Ks = np.linspace(-0.49, -0.43, 33)
     return [M.make_request(int(L), float(Ks[i % 33]), seed=seed0 + i, replica=rank * n + i, n_eq=0,
-                           n_samples=sweeps, sweeps_between=1, n_couplings=2) for i, L in enumerate(Ls)]
+                           n_samples=sweeps, sweeps_between=1, n_couplings=2, update=update)
+            for i, L in enumerate(Ls)]
 
 
 def run_batched(args, D: Dist) -> dict:
@@ -266,7 +268,7 @@ def run_batched(args, D: Dist) -> dict:
     import mcrg_gb300 as M
 
     torch.cuda.set_device(D.local)
-    reqs = batched_requests(M, args.replicas, args.batch_sweeps, D.rank)
+    reqs = batched_requests(M, args.replicas, args.batch_sweeps, D.rank, update=args.update)
     flips = float(sum(r.L * r.L for r in reqs)) * args.batch_sweeps
     creqs = (M._abi.Request * len(reqs))(*reqs)
     for _ in range(args.warmup):
@@ -280,29 +282,40 @@ def run_batched(args, D: Dist) -> dict:
     dt = D.max(time.perf_counter() - t0)
     value = D.world * flips * args.steps / dt / 1e9
     solves = D.world * len(reqs) * args.steps / dt
-    plain = run_plain_subset(M, reqs[: args.plain_subset], D.local)
-    return {"metric": "Gflips/s", "value": round(value, 2), "unit": "Gflips/s", "n_gpus": D.world,
+    plain = run_plain_subset(M, reqs[: args.plain_subset], D.local, args.update)
+    if args.update != "metropolis":  # cluster updates: chain samples (one update + one measurement) per second
+        value = D.world * len(reqs) * args.batch_sweeps * args.steps / dt / 1e6
+        metric = unit = "Msamples/s"
+    else:
+        metric = unit = "Gflips/s"
+    return {"metric": metric, "value": round(value, 2), "unit": unit, "n_gpus": D.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic", "solves_per_s": round(solves, 1),
             "plain": plain, "batched_over_plain_solves": round(solves / D.world / plain["solves_per_s"], 1),
             "config": {"workload": "batched: %d replicas, L in {16..256} (p = .3/.3/.2/.15/.05), K on 33 points in "
-                                   "[-0.49,-0.43], %d sweeps each, measured every sweep, 2 couplings"
-                                   % (args.replicas, args.batch_sweeps),
+                                   "[-0.49,-0.43], %d %s each, measured after every one, 2 couplings"
+                                   % (args.replicas, args.batch_sweeps,
+                                      "sweeps" if args.update == "metropolis" else args.update + " updates"),
                        "parallelism": "replicas x%d" % D.world,
                        "equal_error": "batched and one-per-launch runs give bit-identical moment sums per seed"}}
 
 
-def run_plain_subset(M, reqs, device) -> dict:
+def run_plain_subset(M, reqs, device, update="metropolis") -> dict:
     """The plain GPU path: each request alone, one lattice per launch
-    (mcrg_alloc, mcrg_sweep, mcrg_measure, mcrg_free), back to back."""
+    (mcrg_alloc, mcrg_sweep / mcrg_cluster_update, mcrg_measure / mcrg_measure_cluster,
+    mcrg_free), back to back."""
     import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for r in reqs:
         lat = M.Lattice(r.L, r.K, seed=r.seed, replica=r.replica, n_couplings=r.n_couplings, device=device)
-        lat.sweep(r.n_eq)
-        lat.measure(r.n_samples, r.sweeps_between)
+        if update == "metropolis":
+            lat.sweep(r.n_eq)
+            lat.measure(r.n_samples, r.sweeps_between)
+        else:
+            lat.cluster_update(r.n_eq, update)
+            lat.measure_cluster(r.n_samples, r.sweeps_between, update)
         lat.close()
     dt = time.perf_counter() - t0
     flips = float(sum(r.L * r.L * (r.n_eq + r.n_samples * r.sweeps_between) for r in reqs))
@@ -494,6 +507,8 @@ def main():
     ap.add_argument("--couplings", type=int, default=5)
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--batch-sweeps", type=int, default=1000)
+    ap.add_argument("--update", default="metropolis", choices=["metropolis", "wolff", "sw"],
+                    help="update rule of the batched workload's chains")
     ap.add_argument("--plain-subset", type=int, default=64)
     ap.add_argument("--plain-sweeps", type=int, default=10000)
     ap.add_argument("--served-requests", type=int, default=2000)

@@ -444,8 +444,12 @@ int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between
   if (bins && (bin_size <= 0 || n_bins_cap < 0)) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
   const int nl = c->n_levels, C = c->cfg.n_couplings;
-  // shared-memory contexts: the whole loop in one resident chain launch
-  if (!c->is_tiled && cluster_resident(c->cfg.L, nl, C, c->acc.fast) && (!bins || bin_size <= kMaxDeviceBin))
+  // small shared-memory contexts: the whole loop in one resident chain launch.  From L = 64 on one
+  // chain's CTA is slower per sample than the device-wide kernels (it has few warps and a divergent
+  // union-find); resident cluster chains pay off in batches (mcrg_batch_run, the server), where
+  // many of them fill the GPU.  Both give the same chain.
+  if (!c->is_tiled && c->cfg.L <= 32 && cluster_resident(c->cfg.L, nl, C, c->acc.fast) &&
+      (!bins || bin_size <= kMaxDeviceBin))
     return measure_impl(c, n_samples, updates_between, total, bin_size, bins, n_bins_cap, false, kind);
   if (total) {
     memset(total, 0, sizeof *total);

@@ -85,7 +85,7 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bo
   if (cluster) {  // rcluster::work_bytes(L)
     off = (off + 15) / 16 * 16;
     p.cl_off = off;
-    off += ((L * L * 2 + 15) / 16) * 16 + ((L * L / 8 + 15) / 16) * 16 + 16;
+    off += ((L * L * 2 + 15) / 16) * 16 + 3 * ((L * L / 8 + 15) / 16) * 16 + 16;
   }
   p.bytes = (off + 15) / 16 * 16;
   return p;

@@ -12,7 +12,11 @@
 // a root is always the smallest index of its tree and, once all bonds are
 // united, of its component -- the same roots as the device-wide labelling,
 // hence the same flips.  The lattice is the chain's level 0: bytes (split
-// layout) or bit-plane words.
+// layout) or bit-plane words.  For L >= 32 a warp owns 32-column row
+// segments: the segment's open horizontal bonds are one ballot mask, every
+// site points at the first site of its run, and only vertical bonds (one per
+// pair of runs) and segment-crossing bonds are united, with path halving;
+// a flatten pass leaves every label at its root before the flips.
 #pragma once
 #include "mcrg_planes.cuh"
 
@@ -68,12 +72,27 @@ __device__ __forceinline__ int min16(uint16_t* lab, int x, int b) {
   return b;
 }
 
+// Root of x with path halving (each visited label lowered to its grandparent).
+__device__ __forceinline__ int find_halve16(uint16_t* lab, int x) {
+  const volatile uint16_t* v = lab;
+  for (int it = 0; it < kLoopLimit; ++it) {
+    const int p = v[x];
+    if (p == x) break;
+    const int gp = v[p];
+    if (gp == p) return p;
+    min16(lab, x, gp);
+    x = gp;
+  }
+  return x;
+}
+
 // Links the larger of the two roots under the smaller (retrying while
 // another thread relinks them).
+template <bool HALVE = false>
 __device__ __forceinline__ void unite16(uint16_t* lab, int a, int b) {
   for (int it = 0; it < kLoopLimit; ++it) {
-    a = find16(lab, a);
-    b = find16(lab, b);
+    a = HALVE ? find_halve16(lab, a) : find16(lab, a);
+    b = HALVE ? find_halve16(lab, b) : find16(lab, b);
     if (a == b) return;
     if (a < b) {
       const int t = a;
@@ -86,9 +105,16 @@ __device__ __forceinline__ void unite16(uint16_t* lab, int a, int b) {
   }
 }
 
-// Shared-memory work area of one update: L^2 labels, L^2 / 32 coin words
-// and the seed's root.
-__host__ __device__ inline int work_bytes(int L) { return ((L * L * 2 + 15) / 16) * 16 + ((L * L / 8 + 15) / 16) * 16 + 16; }
+// Shared-memory work area of one update: L^2 labels, L^2 / 32 coin words,
+// the horizontal and vertical bond masks of every 32-column row segment
+// (L >= 32) and the seed's root.
+__host__ __device__ inline int work_bytes(int L) {
+  return ((L * L * 2 + 15) / 16) * 16 + 3 * ((L * L / 8 + 15) / 16) * 16 + 16;
+}
+__device__ __forceinline__ int coin_off(int n) { return ((n * 2 + 15) / 16) * 16; }
+__device__ __forceinline__ int hb_off(int n) { return coin_off(n) + ((n / 8 + 15) / 16) * 16; }
+__device__ __forceinline__ int vb_off(int n) { return hb_off(n) + ((n / 8 + 15) / 16) * 16; }
+__device__ __forceinline__ int seed_off(int n) { return vb_off(n) + ((n / 8 + 15) / 16) * 16; }
 
 // Labels and flips the components of the level's open bonds at update index t.
 // kind: MCRG_UPDATE_WOLFF or MCRG_UPDATE_SWENDSEN_WANG; tb: the bond threshold.
@@ -97,28 +123,69 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
                        int kind, int tid, int T) {
   const int n = L * L, m = L - 1, half = L / 2;
   uint16_t* lab = reinterpret_cast<uint16_t*>(work);
-  uint32_t* coin = reinterpret_cast<uint32_t*>(work + ((n * 2 + 15) / 16) * 16);
-  int* seed_root = reinterpret_cast<int*>(work + ((n * 2 + 15) / 16) * 16 + ((n / 8 + 15) / 16) * 16);
+  uint32_t* coin = reinterpret_cast<uint32_t*>(work + coin_off(n));
+  int* seed_root = reinterpret_cast<int*>(work + seed_off(n));
   const bool wolff = kind == MCRG_UPDATE_WOLFF;
-  for (int x = tid; x < n; x += T) lab[x] = (uint16_t)x;
   if (!wolff)
     for (int x = tid; x < (n + 31) / 32; x += T) coin[x] = 0u;
-  __syncthreads();
-  // open bonds of site pairs (i, j0), (i, j0 + 1): one Philox block each
-  for (int y = tid; y < n / 2; y += T) {
-    const int i = y / half, j0 = 2 * (y - i * half), id = (i + 1) & m, x0 = i * L + j0;
-    const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j0 >> 1), t);
-    const uint32_t s0 = lv.spin(i, j0), s1 = lv.spin(i, j0 + 1);
-    if (r.x < tb && s1 == s0) unite16(lab, x0, x0 + 1);
-    if (r.y < tb && lv.spin(id, j0) == s0) unite16(lab, x0, id * L + j0);
-    if (r.z < tb && lv.spin(i, (j0 + 2) & m) == s1) unite16(lab, x0 + 1, i * L + ((j0 + 2) & m));
-    if (r.w < tb && lv.spin(id, j0 + 1) == s1) unite16(lab, x0 + 1, id * L + j0 + 1);
+  if (L >= 32) {
+    uint32_t* hb = reinterpret_cast<uint32_t*>(work + hb_off(n));
+    uint32_t* vb = reinterpret_cast<uint32_t*>(work + vb_off(n));
+    const int segs = L / 32, units = L * segs, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
+    // runs: unit u = row u / segs, columns 32 (u % segs) .. +31; two units per pass,
+    // lane l draws pair l & 15 of unit 2v + (l >> 4)
+    for (int v = warp; v < units / 2; v += nw) {
+      const int ud = 2 * v + (lane >> 4), di = ud / segs, dj = (ud - di * segs) * 32;
+      const uint4 R = stream_block(key, rep, P_BOND, 0u, (uint32_t)di, (uint32_t)((dj >> 1) + (lane & 15)), t);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int u = 2 * v + h, i = u / segs, j0 = (u - i * segs) * 32, src = h * 16 + (lane >> 1);
+        const uint32_t wx = __shfl_sync(0xFFFFFFFFu, R.x, src), wy = __shfl_sync(0xFFFFFFFFu, R.y, src);
+        const uint32_t wz = __shfl_sync(0xFFFFFFFFu, R.z, src), ww = __shfl_sync(0xFFFFFFFFu, R.w, src);
+        const uint32_t ur = (lane & 1) ? wz : wx, udn = (lane & 1) ? ww : wy;
+        const int j = j0 + lane;
+        const uint32_t s = lv.spin(i, j);
+        const bool right = ur < tb && lv.spin(i, (j + 1) & m) == s;  // lane 31: the bond into the next segment
+        const bool down = udn < tb && lv.spin((i + 1) & m, j) == s;
+        const uint32_t hm = __ballot_sync(0xFFFFFFFFu, right), vm = __ballot_sync(0xFFFFFFFFu, down);
+        const uint32_t starts = ~(hm << 1);
+        const uint32_t low = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+        lab[i * L + j] = (uint16_t)(i * L + j0 + (31 - __clz(starts & low)));
+        if (lane == 0) {
+          hb[u] = hm;
+          vb[u] = vm;
+        }
+      }
+    }
+    __syncthreads();
+    for (int u = warp; u < units; u += nw) {
+      const int i = u / segs, sg = u - i * segs, j0 = sg * 32, in = (i + 1) & m;
+      const uint32_t vv = vb[u], hr = hb[u], hn = hb[in * segs + sg];
+      const uint32_t dup = (vv & hr & hn) << 1;  // column c-1 already joins the same two runs
+      if (((vv & ~dup) >> lane) & 1u) unite16<true>(lab, i * L + j0 + lane, in * L + j0 + lane);
+      if (lane == 31 && (hr >> 31)) unite16<true>(lab, i * L + j0 + 31, i * L + ((j0 + 32) & m));
+    }
+  } else {
+    for (int x = tid; x < n; x += T) lab[x] = (uint16_t)x;
+    __syncthreads();
+    // open bonds of site pairs (i, j0), (i, j0 + 1): one Philox block each
+    for (int y = tid; y < n / 2; y += T) {
+      const int i = y / half, j0 = 2 * (y - i * half), id = (i + 1) & m, x0 = i * L + j0;
+      const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j0 >> 1), t);
+      const uint32_t s0 = lv.spin(i, j0), s1 = lv.spin(i, j0 + 1);
+      if (r.x < tb && s1 == s0) unite16(lab, x0, x0 + 1);
+      if (r.y < tb && lv.spin(id, j0) == s0) unite16(lab, x0, id * L + j0);
+      if (r.z < tb && lv.spin(i, (j0 + 2) & m) == s1) unite16(lab, x0 + 1, i * L + ((j0 + 2) & m));
+      if (r.w < tb && lv.spin(id, j0 + 1) == s1) unite16(lab, x0 + 1, id * L + j0 + 1);
+    }
   }
+  __syncthreads();
+  for (int x = tid; x < n; x += T) lab[x] = (uint16_t)find16(lab, x);  // flatten: every label at its root
   __syncthreads();
   if (wolff) {
     if (tid == 0) {
       const uint4 r = stream_block(key, rep, P_CLUSTER, 0u, 0u, 0u, t);
-      *seed_root = find16(lab, (int)(r.x & (uint32_t)(n - 1)));
+      *seed_root = lab[r.x & (uint32_t)(n - 1)];
     }
   } else {
     for (int x = tid; x < n; x += T)
@@ -129,14 +196,12 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
   __syncthreads();
 }
 
-// Whether site x flips, after update() has labelled the level.
+// Whether site x flips, after update() has labelled the level (labels flattened).
 __device__ __forceinline__ bool flips(const uint8_t* work, int L, int x, bool wolff) {
   const int n = L * L;
-  const uint16_t* lab = reinterpret_cast<const uint16_t*>(work);
-  const uint32_t* coin = reinterpret_cast<const uint32_t*>(work + ((n * 2 + 15) / 16) * 16);
-  const int r = find16(lab, x);
-  if (wolff) return r == *reinterpret_cast<const int*>(work + ((n * 2 + 15) / 16) * 16 + ((n / 8 + 15) / 16) * 16);
-  return (coin[r >> 5] >> (r & 31)) & 1u;
+  const int r = reinterpret_cast<const uint16_t*>(work)[x];
+  if (wolff) return r == *reinterpret_cast<const int*>(work + seed_off(n));
+  return (reinterpret_cast<const uint32_t*>(work + coin_off(n))[r >> 5] >> (r & 31)) & 1u;
 }
 
 // One cluster update of a byte level 0.

@@ -137,10 +137,10 @@ def test_cluster_update_then_sweeps(M):
                                         (256, 3, "sw", KC), (256, 2, "wolff", -0.1), (512, 2, "wolff", KC)])
 def test_measure_cluster_bit_exact(M, L, C, kind, K):
     """mcrg_measure_cluster: n_samples x (updates_between cluster updates + blocking and
-    coupling sums at every level) gives the oracle's moments, bin for bin.  Shared-memory
-    contexts run the whole loop in one resident chain (byte levels, or bit planes in the
-    fast regime, L >= 64); a byte chain of L = 256 does not fit one CTA with its labels and
-    HBM contexts (L = 512) take the per-sample loop of device-wide updates."""
+    coupling sums at every level) gives the oracle's moments, bin for bin.  Contexts up to
+    L = 32 run the whole loop in one resident chain, larger ones the per-sample loop of
+    device-wide updates (the resident form at L >= 64 is checked against it through the
+    batched and served requests below)."""
     seed, rep, ns, ub = 77 + L, 3, 6, 2
     nl = int(math.log2(L)) - 1
     lat = M.Lattice(L, K, seed=seed, replica=rep, n_couplings=C)
