@@ -92,11 +92,11 @@ __device__ __forceinline__ uint4 draw(const Params& P, uint32_t purpose, uint32_
 constexpr int kPackSlots = 8;          // plane-word groups held per colour
 // Open-site queue entries per buffer: one entry per plane word with open
 // sites (about 0.1 per word at the critical coupling, 51 +- 7 of 512); a word
-// that finds its buffer full is resolved by its owner.  The single-slot form
-// (LEAD = 0) keeps 5/32 of the words so that three 512-word CTAs fit an SM.
+// that finds its buffer full is resolved by its owner.
 template <int NT, int LEAD>
 constexpr int queue_cap() {
-  return LEAD == 0 ? NT * 5 / 32 : NT / 4;
+  static_assert(LEAD >= 1, "at least one row group of bulk copies in flight ahead of packing");
+  return NT / 4;
 }
 
 template <int NT, int LEAD>
@@ -278,38 +278,30 @@ __global__ void __launch_bounds__(NT, MINB)
       if (STEADY || p >= 4) qn[(p - 4) % 3] = 0;
       if (STEADY || p >= 7) qn[3 + (p - 7) % 3] = 0;
     }
-    // ---- LEAD = 0: the copy of group p goes out first and lands while the
-    //      phase works on older groups; group p is packed at the end
-    if (LEAD == 0 && tid < 32 && (STEADY || p < J)) issue_group<NS, LW, LEAD>(p, top, b0, b1, ms, in, raw, bar, lane);
     // ---- open sites queued last phase: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6
     {
       const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
       if (STEADY || (g >= 0 && g < J))
         resolve_queue<NS, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
     }
+    // ---- bulk copies of group p + LEAD (its slot was packed last phase)
+    if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
     // ---- pack group p (waits for its copy)
-    auto pack_group = [&]() {
-      if (STEADY || p < J) {
-        if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
+    if (STEADY || p < J) {
+      if (!tma::mbar_wait_bounded(&bar[p % kRawSlots], (uint32_t)((p / kRawSlots) & 1))) ok = false;
 #pragma unroll
-        for (int j = 0; j < WPT; ++j) {
-          const int w = wj[j], off = p * R + rj[j], x = top + off;
-          const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
-          if (STEADY || (x >= b0 - 1 && x <= b1)) {
-            const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
-            pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
-          }
-          if (STEADY || x <= b1 + 1) {
-            const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
-            pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
-          }
+      for (int j = 0; j < WPT; ++j) {
+        const int w = wj[j], off = p * R + rj[j], x = top + off;
+        const int ri = off % RAW_ROWS, pi = off & (PK_ROWS - 1);
+        if (STEADY || (x >= b0 - 1 && x <= b1)) {
+          const uint4* sp = reinterpret_cast<const uint4*>(raw + (size_t)ri * H + 32 * w);
+          pk[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
+        }
+        if (STEADY || x <= b1 + 1) {
+          const uint4* sp = reinterpret_cast<const uint4*>(raw + ((size_t)RAW_ROWS + ri) * H + 32 * w);
+          pk1[pi * WPR + w] = pack_bytes(sp[0], sp[1]);
         }
       }
-    };
-    if (LEAD > 0) {
-      // ---- bulk copies of group p + LEAD (its slot was packed last phase)
-      if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
-      pack_group();
     }
     // ---- colour 0 of group p-2
 #pragma unroll
@@ -361,7 +353,6 @@ __global__ void __launch_bounds__(NT, MINB)
         o1[1] = b;
       }
     }
-    if (LEAD == 0) pack_group();
   };
   // steady phases: groups p (pack), p-2, p-5 and the queues of p-3, p-6 all
   // lie inside the band with every row valid

@@ -161,8 +161,7 @@ struct Variant {
 #define BITS_VARIANT(NT_, MINB_, LEAD_, LW_) BITS_VARIANT_X(NT_, 1, MINB_, LEAD_, LW_)
 // per side: 256 threads x 3 CTAs per SM (copy lead 2), x 4 (lead 1), x 2 (lead 3), 512 x 1, 128 x 4;
 // and 128 threads with two words each (x 4 CTAs per SM, lead 1 or 2).  L = 16384 adds two words per
-// thread at 256 x 2 (lead 1) and 256 x 3 with a single copy slot (lead 0: copy issued at the start of a
-// phase, group packed at its end)
+// thread at 256 x 2 (lead 1)
 #define BITS_VARIANTS_L(LW_)                                                                             \
   BITS_VARIANT(256, 3, 2, LW_), BITS_VARIANT(256, 4, 1, LW_), BITS_VARIANT(256, 2, 3, LW_),             \
       BITS_VARIANT(512, 1, 3, LW_), BITS_VARIANT(128, 4, 3, LW_), BITS_VARIANT_X(128, 2, 4, 1, LW_)
@@ -170,7 +169,7 @@ struct Variant {
 const Variant kVariants[] = {BITS_VARIANT(256, 4, 1, 8),        BITS_VARIANT(256, 3, 2, 8),
                              BITS_VARIANT(256, 2, 3, 8),        BITS_VARIANT(512, 1, 3, 8),
                              BITS_VARIANT_X(128, 2, 4, 1, 8),    BITS_VARIANT_X(128, 2, 4, 2, 8),
-                             BITS_VARIANT_X(256, 2, 2, 1, 8),    BITS_VARIANT_X(256, 2, 3, 0, 8),
+                             BITS_VARIANT_X(256, 2, 2, 1, 8),
                              BITS_VARIANTS_L(7),
                              BITS_VARIANTS_L(6),                 BITS_VARIANTS_L(5),
                              BITS_VARIANTS_L(4),                 BITS_VARIANTS_L(3)};

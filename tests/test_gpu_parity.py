@@ -383,7 +383,7 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
     init = O.init_spins(N, 5, 0)
     ref = O.sweep(init, KC, 5, 0, 0, 1)
     ref_S = O.couplings(ref, 5)
-    for v in ("b256l2", "b256l1", "b512l3", "b128l1x2", "b128l2x2", "b256l1x2", "b256l0x2"):
+    for v in ("b256l2", "b256l1", "b512l3", "b128l1x2", "b128l2x2", "b256l1x2"):
         monkeypatch.setenv("MCRG_TILE", v)
         lat = M.Lattice(N, KC, seed=5, replica=0, n_couplings=5)
         lat.sweep(1)
