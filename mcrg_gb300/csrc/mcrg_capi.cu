@@ -75,6 +75,59 @@ __global__ void split_to_nat_kernel(const uint8_t* __restrict__ split, int N, in
   }
 }
 
+// 32 sites per thread (N >= 32): a natural row segment of 32 int8 +-1 is two
+// 16-byte loads; its even and odd columns become 16 bytes of each colour.
+// A byte is valid iff it is 0x01 or 0xFF: bit 0 set and bits 1..7 all equal.
+__device__ __forceinline__ uint32_t pm1_to_01(uint32_t x, uint32_t& bad) {
+  const uint32_t t = x & 0xFEFEFEFEu;
+  bad |= ((x & 0x01010101u) ^ 0x01010101u) | (t ^ (((t >> 7) & 0x01010101u) * 0xFEu));
+  return (~x >> 7) & 0x01010101u;
+}
+
+__global__ void nat_to_split_vec_kernel(const int8_t* __restrict__ nat, int N, uint8_t* __restrict__ split,
+                                        int* __restrict__ bad) {
+  const int half = N / 2, per_row = N / 32;
+  uint32_t b = 0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < (long long)N * per_row;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q / per_row), j0 = (int)(q - (long long)i * per_row) * 32;
+    const uint4* src = reinterpret_cast<const uint4*>(nat + (size_t)i * N + j0);
+    const uint4 a = src[0], c = src[1];
+    const uint32_t w[8] = {pm1_to_01(a.x, b), pm1_to_01(a.y, b), pm1_to_01(a.z, b), pm1_to_01(a.w, b),
+                           pm1_to_01(c.x, b), pm1_to_01(c.y, b), pm1_to_01(c.z, b), pm1_to_01(c.w, b)};
+    const uint4 ev = make_uint4(__byte_perm(w[0], w[1], 0x6420), __byte_perm(w[2], w[3], 0x6420),
+                                __byte_perm(w[4], w[5], 0x6420), __byte_perm(w[6], w[7], 0x6420));
+    const uint4 od = make_uint4(__byte_perm(w[0], w[1], 0x7531), __byte_perm(w[2], w[3], 0x7531),
+                                __byte_perm(w[4], w[5], 0x7531), __byte_perm(w[6], w[7], 0x7531));
+    const int ce = i & 1;  // the colour whose sites sit on even columns of row i
+    *reinterpret_cast<uint4*>(split + (size_t)ce * N * half + (size_t)i * half + (j0 >> 1)) = ev;
+    *reinterpret_cast<uint4*>(split + (size_t)(1 - ce) * N * half + (size_t)i * half + (j0 >> 1)) = od;
+  }
+  if (b) atomicOr(bad, 1);
+}
+
+__global__ void split_to_nat_vec_kernel(const uint8_t* __restrict__ split, int N, int8_t* __restrict__ nat) {
+  const int half = N / 2, per_row = N / 32;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < (long long)N * per_row;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q / per_row), j0 = (int)(q - (long long)i * per_row) * 32, ce = i & 1;
+    const uint4 e = *reinterpret_cast<const uint4*>(split + (size_t)ce * N * half + (size_t)i * half + (j0 >> 1));
+    const uint4 o = *reinterpret_cast<const uint4*>(split + (size_t)(1 - ce) * N * half + (size_t)i * half + (j0 >> 1));
+    const uint32_t E[4] = {e.x, e.y, e.z, e.w}, O[4] = {o.x, o.y, o.z, o.w};
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      w[2 * k] = __byte_perm(E[k], O[k], 0x5140);
+      w[2 * k + 1] = __byte_perm(E[k], O[k], 0x7362);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] |= (w[k] ^ 0x01010101u) * 0xFFu;  // 1 -> 0x01, 0 -> 0xFF
+    uint4* dst = reinterpret_cast<uint4*>(nat + (size_t)i * N + j0);
+    dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
 __global__ void nat01_kernel(const int8_t* __restrict__ nat, int n, uint8_t* __restrict__ out, int* bad) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int8_t v = nat[s];
@@ -302,7 +355,10 @@ int mcrg_set_spins(mcrg_ctx* c, const int8_t* host) {
   uint8_t* dst = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
   CK(cudaMemcpyAsync(c->d_nat, host, (size_t)L * L, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-  nat_to_split_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
+  if (L >= 32)
+    nat_to_split_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
+  else
+    nat_to_split_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
   CK(cudaGetLastError());
   int bad = 0;
   CK(cudaMemcpyAsync(&bad, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -315,7 +371,10 @@ int mcrg_get_spins(mcrg_ctx* c, int8_t* host) {
   CK(cudaSetDevice(c->cfg.device));
   const int L = c->cfg.L;
   const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
-  split_to_nat_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(src, L, c->d_nat);
+  if (L >= 32)
+    split_to_nat_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(src, L, c->d_nat);
+  else
+    split_to_nat_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(src, L, c->d_nat);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(host, c->d_nat, (size_t)L * L, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
