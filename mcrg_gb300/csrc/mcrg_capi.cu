@@ -348,14 +348,31 @@ int mcrg_free(mcrg_ctx* c) {
   return MCRG_OK;
 }
 
+// Device address of a page-locked, 16-byte-aligned host buffer (the kernels
+// then read or write it directly over the host link), or nullptr for
+// pageable memory, which goes through a staging copy.
+static void* pinned_device_ptr(const void* host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer || ((uintptr_t)a.devicePointer & 15u)) return nullptr;
+  return a.devicePointer;
+}
+
 int mcrg_set_spins(mcrg_ctx* c, const int8_t* host) {
   if (!c || !host) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
   const int L = c->cfg.L;
   uint8_t* dst = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
-  CK(cudaMemcpyAsync(c->d_nat, host, (size_t)L * L, cudaMemcpyHostToDevice, c->stream));
+  const void* direct = L >= 32 ? pinned_device_ptr(host) : nullptr;
+  if (!direct) CK(cudaMemcpyAsync(c->d_nat, host, (size_t)L * L, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-  if (L >= 32)
+  if (direct)  // pinned rows read in place: the copy and the layout conversion are one pass
+    nat_to_split_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(
+        static_cast<const int8_t*>(direct), L, dst, c->d_flag);
+  else if (L >= 32)
     nat_to_split_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
   else
     nat_to_split_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(c->d_nat, L, dst, c->d_flag);
@@ -371,12 +388,15 @@ int mcrg_get_spins(mcrg_ctx* c, int8_t* host) {
   CK(cudaSetDevice(c->cfg.device));
   const int L = c->cfg.L;
   const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
-  if (L >= 32)
+  void* direct = L >= 32 ? pinned_device_ptr(host) : nullptr;
+  if (direct)  // pinned rows written in place
+    split_to_nat_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(src, L, static_cast<int8_t*>(direct));
+  else if (L >= 32)
     split_to_nat_vec_kernel<<<grid_for((int64_t)L * L / 32), 256, 0, c->stream>>>(src, L, c->d_nat);
   else
     split_to_nat_kernel<<<grid_for((int64_t)L * L), 256, 0, c->stream>>>(src, L, c->d_nat);
   CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(host, c->d_nat, (size_t)L * L, cudaMemcpyDeviceToHost, c->stream));
+  if (!direct) CK(cudaMemcpyAsync(host, c->d_nat, (size_t)L * L, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return MCRG_OK;
 }

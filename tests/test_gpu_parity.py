@@ -121,6 +121,31 @@ def test_set_spins_then_sweep(M, N):
     lat.close()
 
 
+@pytest.mark.parametrize("N", [32, 512, 4096])
+def test_spins_through_pinned_host_buffers(M, N):
+    """mcrg_set_spins / mcrg_get_spins with page-locked host rows: the kernels read and
+    write the host buffer in place (one pass for copy and layout conversion); same
+    result as pageable buffers, invalid values still refused."""
+    import ctypes as C
+    import torch
+    from mcrg_gb300 import _abi
+
+    rng = np.random.default_rng(N + 1)
+    s = rand_lattice(rng, N, 0.6)
+    h = torch.empty((N, N), dtype=torch.int8, pin_memory=True)
+    h.copy_(torch.from_numpy(s))
+    lat = M.Lattice(N, KC, seed=12, replica=1)
+    _abi.check(M.lib().mcrg_set_spins(lat._ctx, C.c_void_p(h.data_ptr())), "mcrg_set_spins")
+    np.testing.assert_array_equal(lat.spins_, s)  # pageable read-back
+    lat.sweep(2)
+    out = torch.zeros((N, N), dtype=torch.int8, pin_memory=True)
+    _abi.check(M.lib().mcrg_get_spins(lat._ctx, C.c_void_p(out.data_ptr())), "mcrg_get_spins")
+    np.testing.assert_array_equal(out.numpy(), O.sweep(s, KC, 12, 1, 0, 2))
+    h[N // 2, 3] = 0
+    assert M.lib().mcrg_set_spins(lat._ctx, C.c_void_p(h.data_ptr())) == _abi.EINVAL
+    lat.close()
+
+
 # --------------------------------------------------------------------------
 # measurement: all levels + moment sums
 # --------------------------------------------------------------------------
