@@ -47,7 +47,8 @@ int ilog2i(int x) {
   return l;
 }
 
-int resident_threads(int L) {
+int resident_threads(int L, bool cluster = false) {
+  if (cluster && L >= 64) return L >= 128 ? 512 : 256;  // cluster updates: labelling latency, not occupancy, bounds them
   if (L <= 32) return 32;
   if (L == 64) return 64;
   if (L == 128) return 128;
@@ -99,7 +100,7 @@ void fill_job(ChainJob* j, const mcrg_request* r, int nl, uint8_t* state, mcrg_m
   j->L = r->L;
   j->n_levels = nl;
   j->C = r->n_couplings;
-  j->threads = resident_threads(r->L);
+  j->threads = resident_threads(r->L, r->flags != 0);
   j->key = Key{(uint32_t)r->seed, (uint32_t)(r->seed >> 32)};
   j->replica = r->replica;
   j->init = 1;
