@@ -21,6 +21,8 @@
 // remaining 24 bits from the P_SWEEP_LO stream.  Same-colour sites do not
 // interact, so resolving them after the pass gives the same result as
 // resolving them in place.
+#include <atomic>
+
 #include "mcrg_ops.cuh"
 #include "mcrg_resident_bits.cuh"
 #include "mcrg_resident_cluster.cuh"
@@ -228,14 +230,18 @@ cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels
   constexpr int kMaxSmem = 227 * 1024;  // opt-in shared memory per CTA
   if (plan.bytes > kMaxSmem || threads > 512) return cudaErrorInvalidValue;
   const bool wide = threads > 256;
-  static bool configured[2] = {false, false};  // the attribute is per instantiation, set once to the maximum
-  if (plan.bytes > 48 * 1024 && !configured[wide]) {
-    cudaError_t e = wide ? cudaFuncSetAttribute(chain_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kMaxSmem)
-                         : cudaFuncSetAttribute(chain_kernel<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kMaxSmem);
+  // the attribute belongs to (instantiation, device): one bit per device, set once to the maximum;
+  // host threads may race here, and setting it twice is harmless
+  static std::atomic<uint64_t> configured[2];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = uint64_t(1) << (dev & 63);
+  if (plan.bytes > 48 * 1024 && !(configured[wide].load(std::memory_order_acquire) & bit)) {
+    e = wide ? cudaFuncSetAttribute(chain_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem)
+             : cudaFuncSetAttribute(chain_kernel<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
     if (e != cudaSuccess) return e;
-    configured[wide] = true;
+    configured[wide].fetch_or(bit, std::memory_order_release);
   }
   if (wide) chain_kernel<512, 2><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
   else chain_kernel<256, 3><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);

@@ -140,7 +140,6 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
   for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) J.S[x] = 0ull;
 }
 
-int g_num_sms = 0;
 
 // Variants of the fused sweep: one instantiation per lattice side (L = 64 <<
 // lw) and CTA size; the autotuner picks one per (L, device) by timing each
@@ -192,7 +191,7 @@ void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* o
   if (per_sm < 1) per_sm = 1;
   // bands of at least four row groups, `waves` times as many as fit the GPU at once
   int bands = t->L / (4 * variant_rows(v));
-  if (bands > v.waves * g_num_sms * per_sm) bands = v.waves * g_num_sms * per_sm;
+  if (bands > v.waves * t->sms * per_sm) bands = v.waves * t->sms * per_sm;
   if (bands < 1) bands = 1;
   void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
   cudaLaunchKernel(v.kern, dim3(bands), dim3(block_threads(v)), args, v.smem, s);
@@ -215,11 +214,11 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
   t->replica = replica;
   t->acc = acc;
   if (!acc.fast) return MCRG_ENOSYS;  // the tiled sweep implements the K < -ln2/4 fast path only
-  if (g_num_sms == 0) {
+  {
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 1;
+    cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (t->sms <= 0) t->sms = 1;
   }
   const size_t LL = (size_t)L * L;
   if (cudaMalloc(&t->buf[0], LL) != cudaSuccess || cudaMalloc(&t->buf[1], LL) != cudaSuccess) return MCRG_ENOMEM;
@@ -243,7 +242,7 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
       return MCRG_EIO;
   cudaFuncSetAttribute(tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
   t->variant = -1;
-  tiled_init_kernel<<<g_num_sms * 8, 256, 0, s>>>(t->buf[0], L, key, replica);
+  tiled_init_kernel<<<t->sms * 8, 256, 0, s>>>(t->buf[0], L, key, replica);
   t->cur = 0;
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
 }
@@ -255,7 +254,7 @@ int tiled_reinit(TiledLattice* t, Key key, uint32_t replica, const Accept& acc, 
   t->acc = acc;
   cudaMemsetAsync(t->d_S, 0, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS, s);
   cudaMemsetAsync(t->d_status, 0, sizeof(int), s);
-  tiled_init_kernel<<<g_num_sms * 8, 256, 0, s>>>(t->buf[0], t->L, key, replica);
+  tiled_init_kernel<<<t->sms * 8, 256, 0, s>>>(t->buf[0], t->L, key, replica);
   t->cur = 0;
   return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
 }
@@ -358,7 +357,7 @@ static int measure_one(TiledLattice* t, uint32_t sample, mcrg_moments* bin, bool
     uint8_t* nxt = do_block ? t->levels + t->level_off[l + 1] : nullptr;
     const int64_t work = 2 * (int64_t)n * (n / 32);
     int grid = (int)((work + 255) / 256);
-    if (grid > g_num_sms * 8) grid = g_num_sms * 8;
+    if (grid > t->sms * 8) grid = t->sms * 8;
     if (grid < 1) grid = 1;
     level_kernel<<<grid, 256, 0, s>>>(cur, n, nxt, t->d_S + l * MCRG_MAX_COUPLINGS, t->C, t->key, t->replica, l + 1,
                                       sample, do_block);

@@ -19,6 +19,7 @@ struct TiledLattice {
   mcrg_moments* d_bins = nullptr;
   int64_t bins_cap = 0;
   int variant = -1;                       // sweep variant picked by the autotuner
+  int sms = 0;                            // multiprocessors of the lattice's device
 };
 
 int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica, const Accept& acc,
