@@ -135,7 +135,8 @@ __device__ __forceinline__ uint32_t open_flips(const Params& P, uint32_t c, int 
 }
 
 // Queues plane word w (band offset off) of colour c, which has open sites;
-// returns their flips when the buffer is full (resolved here), else 0.
+// returns their flips when the buffer is full (resolved here), else 0.  (One
+// shared atomic per lane measured faster than a warp-aggregated slot range.)
 template <int NT, int LEAD>
 __device__ __forceinline__ uint32_t enqueue(uint32_t open, uint32_t zero, uint32_t t, int off, int w, int gr,
                                             int c, int qi, int* qn, uint4* Q, const Params& P, uint32_t tt) {
@@ -278,11 +279,13 @@ __global__ void __launch_bounds__(NT, MINB)
       if (STEADY || p >= 4) qn[(p - 4) % 3] = 0;
       if (STEADY || p >= 7) qn[3 + (p - 7) % 3] = 0;
     }
-    // ---- open sites queued last phase: colour 0 of group p-3 (warps 0, 2, ..), colour 1 of group p-6
+    // ---- open sites queued last phase: colour 0 of group p-3, colour 1 of group p-6.  The first
+    //      entries go to the last warps (warp 0 also issues the bulk copies): warp NW-1-k takes
+    //      colour k & 1, entries 32 (k >> 1) + lane, ...
     {
-      const int wi = tid >> 5, c = wi & 1, g = p - (c ? 6 : 3);
+      const int rw = NT / 32 - 1 - (tid >> 5), c = rw & 1, g = p - (c ? 6 : 3);
       if (STEADY || (g >= 0 && g < J))
-        resolve_queue<NS, LW, LEAD>(c, g, (wi >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
+        resolve_queue<NS, LW, LEAD>(c, g, (rw >> 1) * 32 + lane, NT / 2, qn, Q, pk, out, top, ms, P, tt);
     }
     // ---- bulk copies of group p + LEAD (its slot was packed last phase)
     if (tid < 32 && p + LEAD < J) issue_group<NS, LW, LEAD>(p + LEAD, top, b0, b1, ms, in, raw, bar, lane);
