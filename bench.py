@@ -356,8 +356,8 @@ def run_plain(args, D: Dist) -> dict:
 def run_served(args, D: Dist) -> dict:
     """Poisson arrivals of MCRG requests (L log-uniform in {8..1024}, K ~ U[-0.50,-0.42],
     sweeps log-uniform in [1e3, 1e5] scaled by --served-scale) into mcrg_server, at arrival
-    rates swept over 1e2, 1e3 and 1e4 per second (about two seconds of arrivals each, at most
-    --served-requests).  The headline is the solves/s at the highest rate (the server's
+    rates swept over 1e1, 1e2, 1e3 and 1e4 per second (at least 50 requests, about two seconds
+    of arrivals from 1e2/s on, at most --served-requests).  The headline is the solves/s at the highest rate (the server's
     capacity), against the plain one-lattice-per-launch path on a subset of the same mix."""
     import numpy as np
     import torch
@@ -378,7 +378,7 @@ def run_served(args, D: Dist) -> dict:
     srv = M.Server(device=D.local, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)),
                    hbm_workers=args.served_hbm_workers)
     try:
-        for rate in (1e2, 1e3, 1e4):
+        for rate in (1e1, 1e2, 1e3, 1e4):
             n = int(min(args.served_requests, max(50, 2 * rate)))
             reqs = make(n, 100 + 100000 * len(rates))
             all_reqs += reqs
@@ -414,7 +414,7 @@ def run_served(args, D: Dist) -> dict:
             "p50_latency_s": top["p50_latency_s"], "p99_latency_s": top["p99_latency_s"],
             "rates": rates, "plain": plain,
             "served_over_plain_solves": round(top["solves_per_s"] / plain["solves_per_s"], 2),
-            "config": {"workload": "served: Poisson arrivals at 1e2, 1e3, 1e4 /s, L log-uniform {8..1024}, "
+            "config": {"workload": "served: Poisson arrivals at 1e1, 1e2, 1e3, 1e4 /s, L log-uniform {8..1024}, "
                                    "K~U[-0.50,-0.42], sweeps log-uniform [1e3,1e5] x %.3g, slots %d, budget %.0f GB"
                                    % (args.served_scale, args.served_slots, args.served_budget_gb)}}
 
