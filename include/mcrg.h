@@ -19,7 +19,8 @@
  *
  * Monte Carlo update.  The reference grows one Wolff cluster per sample
  * (src/ising.cpp:87-149).  Here one "sweep" updates every site once with a
- * checkerboard Metropolis rule: flip iff always[m] or u32 < thr[m], where
+ * checkerboard Metropolis rule (mcrg_cluster_update / mcrg_measure_cluster
+ * and mcrg_request.flags give the reference's own cluster rule instead): flip iff always[m] or u32 < thr[m], where
  * m = number of anti-aligned neighbours, p[m] = min(1, exp(2K(4-2m))),
  * always[m] = (p[m] == 1), thr[m] = floor(p[m] 2^32).  Both chains sample the
  * same Boltzmann distribution.
@@ -147,7 +148,10 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg);
 int mcrg_free(mcrg_ctx* ctx);
 
 /* Replaces writes / reads of the public Lattice::spins_ (src/lattice.hpp:16;
- * read directly by src/rgnn.cpp:113-114,175).  Values must be +-1. */
+ * read directly by src/rgnn.cpp:113-114,175).  Values must be +-1.  A
+ * page-locked, 16-byte-aligned host buffer (L >= 32) is read / written in
+ * place by the layout-conversion kernel over the host link; other buffers go
+ * through a staging copy.  Both return after the transfer completed. */
 int mcrg_set_spins(mcrg_ctx* ctx, const int8_t* host_spins);
 int mcrg_get_spins(mcrg_ctx* ctx, int8_t* host_spins);
 
