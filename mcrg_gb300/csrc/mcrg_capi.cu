@@ -193,7 +193,7 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   j.L = c->cfg.L;
   j.n_levels = c->n_levels;
   j.C = c->cfg.n_couplings;
-  j.threads = threads_for(c->cfg.L);
+  j.threads = update && c->cfg.L >= 64 ? 512 : threads_for(c->cfg.L);  // cluster labelling is latency-bound
   j.key = Key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
   j.replica = c->cfg.replica;
   j.t0 = (uint32_t)c->t;
@@ -523,11 +523,12 @@ int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between
   if (bins && (bin_size <= 0 || n_bins_cap < 0)) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
   const int nl = c->n_levels, C = c->cfg.n_couplings;
-  // small shared-memory contexts: the whole loop in one resident chain launch.  From L = 64 on one
-  // chain's CTA is slower per sample than the device-wide kernels (it has few warps and a divergent
-  // union-find); resident cluster chains pay off in batches (mcrg_batch_run, the server), where
-  // many of them fill the GPU.  Both give the same chain.
-  if (!c->is_tiled && c->cfg.L <= 32 && cluster_resident(c->cfg.L, nl, C, c->acc.fast) &&
+  // small shared-memory contexts: the whole loop in one resident chain launch.  From L = 128 on one
+  // chain's CTA is slower per sample than the device-wide kernels (measured: 120 / 379 us against
+  // 61 / 68 us per Wolff sample at L = 128 / 256; 47 against 61 us at L = 64); resident cluster
+  // chains pay off in batches (mcrg_batch_run, the server), where many of them fill the GPU.  Both
+  // give the same chain.
+  if (!c->is_tiled && c->cfg.L <= 64 && cluster_resident(c->cfg.L, nl, C, c->acc.fast) &&
       (!bins || bin_size <= kMaxDeviceBin))
     return measure_impl(c, n_samples, updates_between, total, bin_size, bins, n_bins_cap, false, kind);
   if (total) {

@@ -138,7 +138,7 @@ def test_cluster_update_then_sweeps(M):
 def test_measure_cluster_bit_exact(M, L, C, kind, K):
     """mcrg_measure_cluster: n_samples x (updates_between cluster updates + blocking and
     coupling sums at every level) gives the oracle's moments, bin for bin.  Contexts up to
-    L = 32 run the whole loop in one resident chain, larger ones the per-sample loop of
+    L = 64 run the whole loop in one resident chain, larger ones the per-sample loop of
     device-wide updates (the resident form at L >= 64 is checked against it through the
     batched and served requests below)."""
     seed, rep, ns, ub = 77 + L, 3, 6, 2
