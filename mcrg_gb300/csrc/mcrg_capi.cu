@@ -36,6 +36,8 @@ struct mcrg_ctx {
   double* d_rgnn = nullptr;     // forward-pass work: (L/32)^2 + (L/1024)^2 + 3 doubles, the last one the result
   int* d_labels = nullptr;      // cluster updates: L^2 labels (allocated by the first update)
   unsigned long long* d_cl = nullptr;  // cluster updates: [0] flipped spins, [1] error flags
+  mcrg_moments* d_cbins = nullptr;     // cluster measurement: one bin per sample of a chunk
+  ChainJob* d_cjobs = nullptr;         // cluster measurement: one measurement job per sample of a chunk
 };
 
 namespace {
@@ -343,6 +345,8 @@ int mcrg_free(mcrg_ctx* c) {
   cudaFree(c->d_rgnn);
   cudaFree(c->d_labels);
   cudaFree(c->d_cl);
+  cudaFree(c->d_cbins);
+  cudaFree(c->d_cjobs);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MCRG_OK;
@@ -542,14 +546,55 @@ int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between
       bins[q].n_levels = nl;
       bins[q].n_couplings = C;
     }
-  for (int64_t q = 0; q < n_samples; ++q) {
-    int rc = cluster_updates(c, updates_between, kind);
-    if (rc) return rc;
-    mcrg_moments m;  // one measurement, no sweeps (its readback synchronises the stream)
-    rc = measure_impl(c, 1, 0, &m, 0, nullptr, 0, false);
-    if (rc) return rc;
-    if (total) add_moments(total, &m);
-    if (bins && q / bin_size < n_bins_cap) add_moments(&bins[q / bin_size], &m);
+  // chunks of samples: per sample the cluster updates and one measurement into its own device bin,
+  // queued without a host round trip; one read-back per chunk
+  constexpr int64_t kChunk = 256;
+  if (!c->d_cbins && cudaMalloc(&c->d_cbins, sizeof(mcrg_moments) * kChunk) != cudaSuccess) return MCRG_ENOMEM;
+  if (!c->is_tiled && !c->d_cjobs && cudaMalloc(&c->d_cjobs, sizeof(ChainJob) * kChunk) != cudaSuccess)
+    return MCRG_ENOMEM;
+  std::vector<mcrg_moments> h((size_t)kChunk);
+  std::vector<ChainJob> jobs(c->is_tiled ? 0 : (size_t)kChunk);
+  for (int64_t q0 = 0; q0 < n_samples; q0 += kChunk) {
+    const int64_t k = n_samples - q0 < kChunk ? n_samples - q0 : kChunk;
+    CK(cudaMemsetAsync(c->d_cbins, 0, sizeof(mcrg_moments) * (size_t)k, c->stream));
+    if (!c->is_tiled) {  // measurement-only chain jobs (no sweeps, the state is read, not stored)
+      for (int64_t q = 0; q < k; ++q) {
+        ChainJob& j = jobs[(size_t)q];
+        memset(&j, 0, sizeof j);
+        j.L = c->cfg.L;
+        j.n_levels = nl;
+        j.C = C;
+        j.threads = threads_for(c->cfg.L);
+        j.key = Key{(uint32_t)c->cfg.seed, (uint32_t)(c->cfg.seed >> 32)};
+        j.replica = c->cfg.replica;
+        j.n0 = (uint32_t)(c->n + (uint64_t)q);
+        j.n_samples = 1;
+        j.bin_size = 1;
+        j.state = c->d_state;
+        j.bins = c->d_cbins + q;
+        j.acc = c->acc;
+      }
+      CK(cudaMemcpyAsync(c->d_cjobs, jobs.data(), sizeof(ChainJob) * (size_t)k, cudaMemcpyHostToDevice,
+                         c->stream));
+    }
+    for (int64_t q = 0; q < k; ++q) {
+      int rc = cluster_updates(c, updates_between, kind);
+      if (rc) return rc;
+      if (c->is_tiled) {
+        rc = tiled_measure_sample(&c->tiled, (uint32_t)(c->n + (uint64_t)q), c->d_cbins + q, c->stream);
+        if (rc) return rc;
+      } else {
+        CK(launch_chain(c->d_cjobs + q, 1, c->cfg.L, nl, C, jobs[0].threads, c->acc.fast && c->cfg.L >= 64,
+                        c->stream));
+      }
+    }
+    CK(cudaMemcpyAsync(h.data(), c->d_cbins, sizeof(mcrg_moments) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->n += (uint64_t)k;
+    for (int64_t q = 0; q < k; ++q) {
+      if (total) add_moments(total, &h[(size_t)q]);
+      if (bins && (q0 + q) / bin_size < n_bins_cap) add_moments(&bins[(q0 + q) / bin_size], &h[(size_t)q]);
+    }
   }
   return cluster_readback(c, nullptr);
 }

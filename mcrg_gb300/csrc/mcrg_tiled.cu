@@ -403,6 +403,10 @@ int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, 
   return MCRG_OK;
 }
 
+int tiled_measure_sample(TiledLattice* t, uint32_t sample, mcrg_moments* bin, cudaStream_t s) {
+  return measure_one(t, sample, bin, false, s);
+}
+
 int tiled_status(TiledLattice* t, cudaStream_t s) {
   int h = 0;
   if (cudaMemcpyAsync(&h, t->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;

@@ -37,6 +37,9 @@ int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s);
 int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, int64_t sweeps_between,
                   int64_t bin_size, int64_t* n_bins, cudaStream_t s, bool flow = false);
 mcrg_moments* tiled_bins(TiledLattice* t);
+// One measurement of the current configuration (no sweeps) at tie-stream
+// sample index `sample`, added into *bin (device; n_samples counts it).
+int tiled_measure_sample(TiledLattice* t, uint32_t sample, mcrg_moments* bin, cudaStream_t s);
 // Sweep schedule in use (after the first sweep): rows per pipeline group
 // and threads per CTA; returns the variant index.
 int tiled_variant(TiledLattice* t, int* rows, int* threads);
