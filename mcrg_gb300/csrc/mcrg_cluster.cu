@@ -18,7 +18,8 @@
 //   2. cl_merge_kernel (L > 32): every open bond that crosses a tile edge
 //      unites the two trees of the global forest; atomicMin links the larger
 //      root under the smaller, so a root is always the smallest index of its
-//      tree and, at the end, of its cluster;
+//      tree and, at the end, of its cluster (finds halve the paths they walk:
+//      a cluster spanning thousands of tiles would otherwise leave long chains);
 //   3. cl_flip_kernel: every site finds its root; Wolff flips the sites that
 //      share the seed's root, Swendsen-Wang the sites whose root draws a set
 //      bit; the flips are counted.  With T = 32 a CTA loads its tile's labels
@@ -210,14 +211,14 @@ __global__ void __launch_bounds__(256) cl_merge_kernel(const uint8_t* __restrict
       const int i = (int)(e / tpr), j = (int)(e - (long long)i * tpr) * kTile + kTile - 1;  // odd
       const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j >> 1), t);
       if (r.z < tb && nat_spin(st, L, i, j) == nat_spin(st, L, i, (j + 1) & m))
-        unite(label, i * L + j, i * L + ((j + 1) & m), err);
+        unite<true>(label, i * L + j, i * L + ((j + 1) & m), err);
     } else {
       const long long e2 = e - right;
       const int i = (int)(e2 / L) * kTile + kTile - 1, j = (int)(e2 - (e2 / L) * L);
       const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j >> 1), t);
       const uint32_t u = (j & 1) ? r.w : r.y;
       if (u < tb && nat_spin(st, L, i, j) == nat_spin(st, L, (i + 1) & m, j))
-        unite(label, i * L + j, ((i + 1) & m) * L + j, err);
+        unite<true>(label, i * L + j, ((i + 1) & m) * L + j, err);
     }
   }
 }
@@ -235,7 +236,7 @@ __device__ __forceinline__ uint32_t even_bits(uint32_t x) {
 // in-tile component are resolved once, then every site looks them up; a
 // warp owns a tile row and applies its flips as two 16-byte XORs.
 __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st, int L, int lg,
-                                                        const int* __restrict__ label, int kind, Key key, uint32_t rep,
+                                                        int* label, int kind, Key key, uint32_t rep,
                                                         uint32_t t, unsigned long long* count, int* err) {
   __shared__ int lbl[1024], groot[1024];
   __shared__ uint8_t need[1024], coin[1024];
@@ -246,7 +247,7 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
   const bool wolff = kind == MCRG_UPDATE_WOLFF;
   if (wolff && threadIdx.x == 0) {
     const uint4 r = stream_block(key, rep, P_CLUSTER, 0u, 0u, 0u, t);
-    seed_root = find_root(label, (int)(r.x & (uint32_t)(L * L - 1)), err);
+    seed_root = find_halve(label, (int)(r.x & (uint32_t)(L * L - 1)), err);
   }
   for (int x = threadIdx.x; x < 1024; x += 256) need[x] = 0;
   __syncthreads();
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
   __syncthreads();
   for (int x = threadIdx.x; x < 1024; x += 256)
     if (need[x]) {
-      const int r = find_root(label, ((i0 + (x >> 5)) << lg) + j0 + (x & 31), err);
+      const int r = find_halve(label, ((i0 + (x >> 5)) << lg) + j0 + (x & 31), err);
       groot[x] = r;
       if (!wolff)
         coin[x] = (uint8_t)(stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)r >> 16, (uint32_t)r & 0xFFFFu, t).x & 1u);
@@ -278,7 +279,7 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
     if (q >= 0) {
       flip = wolff ? groot[q] == seed_root : coin[q] != 0;
     } else {  // a tile root the merge linked elsewhere: its own root
-      const int g = find_root(label, v, err);
+      const int g = find_halve(label, v, err);
       flip = wolff ? g == seed_root
                    : (stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)g >> 16, (uint32_t)g & 0xFFFFu, t).x & 1u) != 0;
     }
