@@ -21,6 +21,9 @@
 // remaining 24 bits from the P_SWEEP_LO stream.  Same-colour sites do not
 // interact, so resolving them after the pass gives the same result as
 // resolving them in place.
+// Cluster chains (ChainJob.update = Wolff / Swendsen-Wang, L <= 256): each
+// Monte Carlo step is a cluster update of level 0 in shared memory
+// (mcrg_resident_cluster.cuh) instead of a sweep; the measurement is the same.
 #include <atomic>
 
 #include "mcrg_ops.cuh"
