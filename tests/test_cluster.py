@@ -315,3 +315,31 @@ def test_cluster_updates_decorrelate_faster(M):
     for k in ("sw", "wolff"):
         d = means[k][0] - means["metropolis"][0]
         assert abs(d) < 5 * math.hypot(means[k][1], means["metropolis"][1]), (k, means)
+
+
+@pytest.mark.gpu
+def test_cluster_api_errors(M):
+    """Invalid update kinds and counts are refused without touching the chain; zero
+    updates are a no-op; a batched request with an unknown update rule fails alone."""
+    import ctypes as C
+    from mcrg_gb300 import _abi
+
+    lat = M.Lattice(16, KC, seed=1)
+    s0 = lat.spins_
+    f = C.c_int64(-1)
+    assert M.lib().mcrg_cluster_update(lat._ctx, 1, 7, C.byref(f)) == _abi.EINVAL
+    assert M.lib().mcrg_cluster_update(lat._ctx, -1, 1, C.byref(f)) == _abi.EINVAL
+    assert M.lib().mcrg_cluster_update(lat._ctx, 0, 1, C.byref(f)) == 0 and f.value == 0
+    tot = _abi.Moments()
+    assert M.lib().mcrg_measure_cluster(lat._ctx, 2, 1, 9, C.byref(tot), 0, None, 0) == _abi.EINVAL
+    assert M.lib().mcrg_measure_cluster(lat._ctx, 2, -1, 1, C.byref(tot), 0, None, 0) == _abi.EINVAL
+    np.testing.assert_array_equal(lat.spins_, s0)
+    assert lat.counters() == (0, 0)
+    with pytest.raises(ValueError):
+        lat.cluster_update(1, "metropolis")
+    lat.close()
+    bad = M.make_request(16, KC, 1, n_samples=1)
+    bad.flags = 5
+    good = M.make_request(16, KC, 2, n_samples=1, update="wolff")
+    res = M.batch_run([bad, good])
+    assert res[0][0] == _abi.EINVAL and res[1][0] == 0
