@@ -238,9 +238,9 @@ __device__ __forceinline__ uint32_t even_bits(uint32_t x) {
 __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st, int L, int lg,
                                                         int* label, int kind, Key key, uint32_t rep,
                                                         uint32_t t, unsigned long long* count, int* err) {
-  __shared__ int lbl[1024], groot[1024];
+  __shared__ int lbl[1024], groot[1024], todo[1024];
   __shared__ uint8_t need[1024], coin[1024];
-  __shared__ int seed_root;
+  __shared__ int seed_root, n_todo;
   __shared__ unsigned long long warp_cnt[8];
   const int tpr = L >> 5, ti = blockIdx.x >> (lg - 5), tj = blockIdx.x & (tpr - 1);
   const int i0 = ti << 5, j0 = tj << 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
     seed_root = find_halve(label, (int)(r.x & (uint32_t)(L * L - 1)), err);
   }
   for (int x = threadIdx.x; x < 1024; x += 256) need[x] = 0;
+  if (threadIdx.x == 0) n_todo = 0;
   __syncthreads();
   // the in-tile index of a label, or -1 when it lies outside the tile
   auto loc = [&](int v) {
@@ -263,13 +264,24 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
     if (q >= 0) need[q] = 1;
   }
   __syncthreads();
-  for (int x = threadIdx.x; x < 1024; x += 256)
-    if (need[x]) {
-      const int r = find_halve(label, ((i0 + (x >> 5)) << lg) + j0 + (x & 31), err);
-      groot[x] = r;
-      if (!wolff)
-        coin[x] = (uint8_t)(stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)r >> 16, (uint32_t)r & 0xFFFFu, t).x & 1u);
-    }
+  // the in-tile components' roots as a dense list (one shared atomic per warp and pass), so that
+  // their global root lookups and coins keep every lane busy
+  for (int x = threadIdx.x; x < 1024; x += 256) {
+    const bool nd = need[x] != 0;
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, nd);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&n_todo, __popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (nd) todo[base + __popc(m & ((1u << lane) - 1u))] = x;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n_todo; e += 256) {
+    const int x = todo[e];
+    const int r = find_halve(label, ((i0 + (x >> 5)) << lg) + j0 + (x & 31), err);
+    groot[x] = r;
+    if (!wolff)
+      coin[x] = (uint8_t)(stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)r >> 16, (uint32_t)r & 0xFFFFu, t).x & 1u);
+  }
   __syncthreads();
   const int h = L / 2;
   unsigned cnt = 0;
