@@ -222,6 +222,11 @@ int mcrg_measure_cluster(mcrg_ctx* ctx, int64_t n_samples, int64_t updates_betwe
 
 /* Sweep and sample counters (the Philox time words of the next sweep / sample). */
 int mcrg_counters(mcrg_ctx* ctx, uint64_t* sweeps, uint64_t* samples);
+/* Sets them: with mcrg_set_spins, a context of the same mcrg_cfg resumes a
+ * saved chain (mcrg_get_spins + mcrg_counters) exactly, draw for draw.  The
+ * reference has no checkpoint (its only persistence is the final spin dump of
+ * Lattice::write_spins, src/lattice.cpp:63-75). */
+int mcrg_set_counters(mcrg_ctx* ctx, uint64_t sweeps, uint64_t samples);
 /* Sweep schedule the autotuner picked for an HBM-resident context: rows per
  * pipeline group (tile_rows) and threads per CTA (tile_cols); MCRG_EINVAL
  * for shared-memory-resident contexts and MCRG_EAGAIN before the first
@@ -311,6 +316,11 @@ typedef struct mcrg_server mcrg_server;
 int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg);
 int mcrg_submit(mcrg_server* srv, const mcrg_request* req, uint64_t* ticket);
 int mcrg_poll(mcrg_server* srv, uint64_t ticket, mcrg_result* out);   /* MCRG_EAGAIN while running */
+/* Withdraws a request that is still queued: its result (mcrg_poll / mcrg_wait)
+ * has status MCRG_ECANCELED.  MCRG_EBUSY once it is admitted (its chain runs
+ * to the end), MCRG_EINVAL when it has finished, MCRG_ENOENT for an unknown
+ * ticket.  No counterpart in the reference. */
+int mcrg_cancel(mcrg_server* srv, uint64_t ticket);
 int mcrg_wait(mcrg_server* srv, uint64_t ticket, double timeout_s, mcrg_result* out);
 int mcrg_server_stats(mcrg_server* srv, int64_t* admitted, int64_t* completed, int64_t* in_flight,
                       int64_t* bytes_in_use);

@@ -176,6 +176,16 @@ class Lattice:
         check(lib().mcrg_counters(self._ctx, C.byref(t), C.byref(n)), "mcrg_counters")
         return int(t.value), int(n.value)
 
+    def checkpoint(self) -> dict:
+        """The chain's state: configuration and Philox counters (restore() on a Lattice
+        of the same L, K, seed, replica and levels continues it exactly)."""
+        t, n = self.counters()
+        return {"spins": self.spins_, "sweeps": t, "samples": n}
+
+    def restore(self, ckpt: dict) -> None:
+        self.spins_ = ckpt["spins"]
+        check(lib().mcrg_set_counters(self._ctx, int(ckpt["sweeps"]), int(ckpt["samples"])), "mcrg_set_counters")
+
     def tile_shape(self):
         """(rows per pipeline group, threads per CTA) of the autotuned HBM sweep,
         or None for shared-memory-resident lattices."""
@@ -347,6 +357,10 @@ class Server:
             return None
         check(rc, "mcrg_poll")
         return r
+
+    def cancel(self, ticket: int) -> None:
+        """Withdraw a queued request (MCRGError EBUSY once it is running)."""
+        check(lib().mcrg_cancel(self._h, ticket), "mcrg_cancel")
 
     def wait(self, ticket: int, timeout_s: float = 60.0):
         r = _abi.Result()

@@ -82,6 +82,8 @@ _SIGS = {
     "mcrg_interactions": (C.c_int, [C.c_void_p, P(C.c_int64)]),
     "mcrg_measure": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(Moments), C.c_int64, P(Moments), C.c_int64]),
     "mcrg_measure_flow": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, P(FlowMoments)]),
+    "mcrg_set_counters": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
+    "mcrg_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "mcrg_cluster_update": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, P(C.c_int64)]),
     "mcrg_measure_cluster": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32, P(Moments), C.c_int64,
                                        P(Moments), C.c_int64]),

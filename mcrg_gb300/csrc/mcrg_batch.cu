@@ -623,6 +623,26 @@ int mcrg_submit(mcrg_server* s, const mcrg_request* r, uint64_t* ticket) {
   return MCRG_OK;
 }
 
+int mcrg_cancel(mcrg_server* s, uint64_t ticket) {
+  if (!s) return MCRG_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (auto it = s->pending.begin(); it != s->pending.end(); ++it)
+    if (it->ticket == ticket) {  // not admitted yet: it never reaches the device
+      mcrg_result res;
+      memset(&res, 0, sizeof res);
+      res.status = MCRG_ECANCELED;
+      res.submit_s = it->submit_s;
+      res.done_s = mono_s();
+      s->done[ticket] = res;
+      s->submitted.erase(ticket);
+      s->pending.erase(it);
+      s->cv_done.notify_all();
+      return MCRG_OK;
+    }
+  if (s->submitted.count(ticket)) return MCRG_EBUSY;  // admitted: its chain is on the device
+  return s->done.count(ticket) ? MCRG_EINVAL : MCRG_ENOENT;  // finished (result not collected yet) / unknown
+}
+
 int mcrg_poll(mcrg_server* s, uint64_t ticket, mcrg_result* out) {
   if (!s || !out) return MCRG_EINVAL;
   std::lock_guard<std::mutex> lk(s->mu);

@@ -691,6 +691,13 @@ int mcrg_interactions(mcrg_ctx* c, int64_t* out) {
   return MCRG_OK;
 }
 
+int mcrg_set_counters(mcrg_ctx* c, uint64_t sweeps, uint64_t samples) {
+  if (!c || sweeps > 0xFFFFFFFFull || samples > 0xFFFFFFFFull) return MCRG_EINVAL;  // 32-bit Philox time words
+  c->t = sweeps;
+  c->n = samples;
+  return MCRG_OK;
+}
+
 int mcrg_counters(mcrg_ctx* c, uint64_t* sweeps, uint64_t* samples) {
   if (!c) return MCRG_EINVAL;
   if (sweeps) *sweeps = c->t;

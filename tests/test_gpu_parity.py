@@ -418,3 +418,64 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
         assert np.array_equal(got, ref), "variant %s differs at %d sites" % (v, int((got != ref).sum()))
         np.testing.assert_array_equal(S[0], ref_S)
         del got
+
+
+# --------------------------------------------------------------------------
+# checkpoint / resume and request cancellation
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("N,rule", [(32, "metropolis"), (512, "metropolis"), (64, "wolff"), (512, "sw")])
+def test_checkpoint_resume_is_exact(M, N, rule):
+    """A chain saved (spins + Philox counters) and restored into a fresh context of the same
+    configuration continues exactly as the original one does."""
+    def advance(lat, k):
+        if rule == "metropolis":
+            lat.sweep(2)
+            return lat.measure(k, 1)[0]
+        lat.cluster_update(2, rule)
+        return lat.measure_cluster(k, 1, rule)[0]
+
+    a = M.Lattice(N, KC, seed=61, replica=3, n_couplings=2)
+    advance(a, 3)
+    ckpt = a.checkpoint()
+    tot_a = advance(a, 4)
+    b = M.Lattice(N, KC, seed=61, replica=3, n_couplings=2)
+    b.restore(ckpt)
+    assert b.counters() == (ckpt["sweeps"], ckpt["samples"])
+    tot_b = advance(b, 4)
+    assert_moments_equal(tot_a, tot_b)
+    np.testing.assert_array_equal(a.spins_, b.spins_)
+    assert a.counters() == b.counters()
+    a.close()
+    b.close()
+
+
+def test_server_cancel(M):
+    """A queued request can be withdrawn (its result says ECANCELED); a running one cannot;
+    the requests around it are unaffected."""
+    from mcrg_gb300 import _abi
+
+    srv = M.Server(slots=1, hbm_budget_bytes=64 << 20)
+    try:
+        t1 = srv.submit(M.make_request(64, KC, 1, n_eq=200000, n_samples=1))
+        import time
+        time.sleep(0.05)  # let the scheduler admit it
+        r3 = M.make_request(16, KC, 3, n_eq=2, n_samples=3)
+        t2 = srv.submit(M.make_request(8, KC, 2, n_samples=1))
+        t3 = srv.submit(r3)
+        srv.cancel(t2)
+        assert srv.wait(t2, 10).status == _abi.ECANCELED
+        with pytest.raises(M.MCRGError) as e:
+            srv.cancel(t1)
+        assert e.value.code == _abi.EBUSY
+        out3 = srv.wait(t3, 60)
+        assert out3.status == 0
+        lat = M.Lattice(16, KC, seed=3)
+        lat.sweep(2)
+        assert_moments_equal(M.moments_from_c(out3.moments), lat.measure(3, 1)[0])
+        lat.close()
+        assert srv.wait(t1, 60).status == 0
+        with pytest.raises(M.MCRGError) as e:
+            srv.cancel(987654)
+        assert e.value.code == _abi.ENOENT
+    finally:
+        srv.close()
