@@ -323,6 +323,43 @@ def run_plain_subset(M, reqs, device, update="metropolis") -> dict:
             "requests": len(reqs), "seconds": round(dt, 3)}
 
 
+def run_cluster(args, D: Dist) -> dict:
+    """Cluster updates of one lattice of side --L (the reference's update rule on the
+    device): --update wolff or sw (metropolis selects sw), equilibrated first with
+    Swendsen-Wang updates at K = Kc; a step is --cluster-updates updates."""
+    import torch
+    import mcrg_gb300 as M
+    torch.cuda.set_device(D.local)
+    kind = "sw" if args.update == "metropolis" else args.update
+    L, n = args.L, args.cluster_updates
+    lat = M.Lattice(L, KC, seed=11, replica=D.rank, n_couplings=2, device=D.local)
+    lat.cluster_update(args.cluster_equilibrate, "sw")
+    for _ in range(args.warmup):
+        lat.cluster_update(n, kind)
+    stream = torch.cuda.ExternalStream(lat.stream(), device=D.local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    D.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    flipped = 0
+    for _ in range(args.steps):
+        flipped += lat.cluster_update(n, kind)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = D.max(e0.elapsed_time(e1))
+    lat.close()
+    updates = args.steps * n
+    return {"metric": "Gsites/s", "value": round(D.world * L * L * updates / (ms * 1e-3) / 1e9, 2),
+            "unit": "Gsites/s", "n_gpus": D.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 3), "ms_per_update": round(ms / updates, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "flipped_fraction": round(flipped / updates / (L * L), 4),
+            "config": {"workload": "cluster: one L=%d lattice, %s updates at K=Kc after %d Swendsen-Wang updates; "
+                                   "Gsites/s = lattice sites per update x updates per second"
+                                   % (L, kind, args.cluster_equilibrate), "L": L, "update": kind}}
+
+
 def run_plain(args, D: Dist) -> dict:
     """One L = 64 lattice, one CTA per launch, 5 couplings (plain GPU config)."""
     import torch
@@ -501,14 +538,16 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="large", choices=["large", "batched", "plain", "served"])
+    ap.add_argument("--workload", default="large", choices=["large", "batched", "plain", "served", "cluster"])
     ap.add_argument("--L", type=int, default=16384)
     ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--couplings", type=int, default=5)
     ap.add_argument("--replicas", type=int, default=4096)
     ap.add_argument("--batch-sweeps", type=int, default=1000)
     ap.add_argument("--update", default="metropolis", choices=["metropolis", "wolff", "sw"],
-                    help="update rule of the batched workload's chains")
+                    help="update rule of the batched workload's chains (cluster workload: wolff or sw)")
+    ap.add_argument("--cluster-updates", type=int, default=10, help="cluster workload: updates per step")
+    ap.add_argument("--cluster-equilibrate", type=int, default=60, help="cluster workload: SW updates first")
     ap.add_argument("--plain-subset", type=int, default=64)
     ap.add_argument("--plain-sweeps", type=int, default=10000)
     ap.add_argument("--served-requests", type=int, default=2000)
@@ -549,8 +588,9 @@ def main():
         print(json.dumps(out), flush=True)
         return
 
-    out = {"large": run_large, "batched": run_batched, "plain": run_plain, "served": run_served}[args.workload](args, D)
-    if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline:
+    out = {"large": run_large, "batched": run_batched, "plain": run_plain, "served": run_served,
+           "cluster": run_cluster}[args.workload](args, D)
+    if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline and args.workload != "cluster":
         threads = cpu_threads(args.L)
         cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads)
         out["cpu_baseline"] = {"value": round(cb["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": threads,
