@@ -25,7 +25,8 @@ from ._abi import MCRGError, check, lib
 from .tmatrix import MomentSums, eigenvalues, jackknife, nu
 
 __all__ = ["Lattice", "IsingModel", "MonteCarloRenormalizationGroup", "MomentSums", "batch_run", "Server",
-           "block_lattice", "lattice_couplings", "thresholds", "moments_from_c", "MCRGError", "lib"]
+           "block_lattice", "lattice_couplings", "thresholds", "moments_from_c", "MCRGError", "lib",
+           "nearest_neighbors", "next_nearest_neighbors"]
 
 KC = -math.log(1.0 + math.sqrt(2.0)) / 2.0
 
@@ -65,6 +66,7 @@ class Lattice:
     def __init__(self, N: int, K: float = KC, seed: int = 1, replica: int = 0, n_levels: int = -1,
                  n_couplings: int = 2, device: int = 0, b: int = 2):
         self._ctx = None
+        self._site_rng = np.random.default_rng([seed & 0xFFFFFFFFFFFFFFFF, replica])
         cfg = _abi.Cfg(N, b, n_levels, n_couplings, float(K), seed & 0xFFFFFFFFFFFFFFFF, replica, device)
         h = C.c_void_p()
         check(lib().mcrg_alloc(C.byref(h), C.byref(cfg)), "mcrg_alloc")
@@ -75,6 +77,16 @@ class Lattice:
         self.K = float(K)
         self.n_couplings = n_couplings
         self.n_levels = n_levels if n_levels >= 0 else int(math.log2(N)) - 1
+
+    @classmethod
+    def from_spins(cls, a: int, spins: np.ndarray, K: float = KC, seed: int = 1, **kw) -> "Lattice":
+        """Lattice(a, spins) (src/lattice.cpp:18-31): a lattice of spacing a holding the
+        given +-1 configuration."""
+        spins = np.asarray(spins)
+        lat = cls(spins.shape[0], K, seed, **kw)
+        lat.a_ = int(a)
+        lat.spins_ = spins
+        return lat
 
     def __del__(self):
         self.close()
@@ -115,6 +127,42 @@ class Lattice:
     def calc_interactions(self) -> np.ndarray:
         """Level-0 (S_nn, S_nnn, ...) as src/lattice.cpp:102-120 returns them."""
         return self.interactions()[0]
+
+    def calc_nearest_neighbor_interaction(self) -> float:
+        """S_nn of the current configuration (src/lattice.cpp:84-99)."""
+        return float(self.interactions()[0][0])
+
+    def write_spins(self, f) -> None:
+        """src/lattice.cpp:63-75: a blank line, then one "# s, s, ..., " line per row."""
+        from .logfiles import spin_lines
+
+        f.write("\n" + "".join(l + "\n" for l in spin_lines(self.spins_)))
+
+    def display_spins(self) -> None:
+        """src/lattice.cpp:44-60: the configuration as coloured O (+1) / X (-1)."""
+        up, down = "\033[34m%2s\033[0m" % "O", "\033[37m%2s\033[0m" % "X"
+        for row in self.spins_:
+            print("".join(up if v == 1 else down for v in row))
+        print("(Lattice spacing a = %d)\n" % self.a_)
+
+    def choose_random_spin(self) -> int:
+        """src/lattice.cpp:78-81: a uniform site index in [0, N^2) (host generator
+        seeded from seed and replica)."""
+        return int(self._site_rng.integers(0, self.n_spins_))
+
+    def nearest_neighbors(self, i: int, j: int) -> np.ndarray:
+        return nearest_neighbors(self.N_, i, j)
+
+    def next_nearest_neighbors(self, i: int, j: int) -> np.ndarray:
+        return next_nearest_neighbors(self.N_, i, j)
+
+    def advance(self, n: int, update: str = "metropolis") -> None:
+        """n Monte Carlo steps of the given rule: "metropolis" sweeps, or "wolff" /
+        "sw" cluster updates on the device."""
+        if _update_kind(update) == 0:
+            self.sweep(n)
+        else:
+            self.cluster_update(n, update)
 
     def measure(self, n_samples: int, sweeps_between: int = 1, bin_size: int = 0):
         """Sample loop of src/mcrg.cpp:72-98 on the device; returns (total, bins)."""
@@ -202,25 +250,49 @@ class Lattice:
         check(lib().mcrg_sync(self._ctx), "mcrg_sync")
 
 
-class IsingModel:
-    """IsingModel(K) (src/ising.hpp:8-41): the update rule is the device sweep."""
+def nearest_neighbors(N: int, i: int, j: int) -> np.ndarray:
+    """Lattice::nearest_neighbors (src/lattice.cpp:124-136): the periodic neighbours
+    (i+1, j), (i-1, j), (i, j+1), (i, j-1) of site (i, j) as a 4 x 2 array."""
+    return np.array([[(i + 1) % N, j], [(i - 1) % N, j], [i, (j + 1) % N], [i, (j - 1) % N]], dtype=np.int64)
 
-    def __init__(self, K: float):
+
+def next_nearest_neighbors(N: int, i: int, j: int) -> np.ndarray:
+    """Lattice::next_nearest_neighbors (src/lattice.cpp:139-151): the diagonal
+    neighbours (i+1, j+1), (i-1, j+1), (i+1, j-1), (i-1, j-1)."""
+    return np.array([[(i + 1) % N, (j + 1) % N], [(i - 1) % N, (j + 1) % N],
+                     [(i + 1) % N, (j - 1) % N], [(i - 1) % N, (j - 1) % N]], dtype=np.int64)
+
+
+def _update_kind(update) -> int:
+    if isinstance(update, str) and update.lower() in ("metropolis", "sweep", "checkerboard"):
+        return 0
+    return _cluster_kind(update)
+
+
+class IsingModel:
+    """IsingModel(K) (src/ising.hpp:8-41).  update_ selects the Monte Carlo step:
+    "metropolis" (default: one checkerboard sweep, same stationary distribution as
+    the reference's step), "wolff" (the reference's own rule, src/ising.cpp:87-155,
+    on the device) or "sw" (Swendsen-Wang)."""
+
+    def __init__(self, K: float, update: str = "metropolis"):
         self.K_ = float(K)
-        self.P_ = 1.0 - math.exp(2.0 * K)  # kept for API parity (Wolff bond probability)
+        self.P_ = 1.0 - math.exp(2.0 * K)  # Wolff bond probability (src/ising.cpp:9)
+        _update_kind(update)
+        self.update_ = update
 
     def equilibrate(self, lattice: Lattice, n_samples_eq: int, write: bool = False) -> None:
         """src/ising.cpp:14-84; with write, logs equilibrate_N_<N>_K_<K>.txt in the
         reference's format (see mcrg_gb300.logfiles)."""
         if not write:
-            lattice.sweep(n_samples_eq)
+            lattice.advance(n_samples_eq, self.update_)
             return
         from .logfiles import write_equilibrate
 
         write_equilibrate(self, lattice, n_samples_eq)
 
     def sample_new_configuration(self, lattice: Lattice) -> None:
-        lattice.sweep(1)
+        lattice.advance(1, self.update_)
 
     def calc_energy(self, lattice: Lattice) -> float:
         return self.K_ * float(lattice.calc_interactions()[0]) / (lattice.N_ * lattice.N_)

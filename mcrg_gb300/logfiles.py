@@ -31,6 +31,11 @@ def nn_sum(spins: np.ndarray) -> int:
     return int((s * (np.roll(s, 1, 0) + np.roll(s, -1, 0) + np.roll(s, 1, 1) + np.roll(s, -1, 1))).sum())
 
 
+def spin_lines(spins: np.ndarray) -> list[str]:
+    """The rows of Lattice::write_spins (src/lattice.cpp:63-75): "# s, s, ..., "."""
+    return ["# " + "".join("%d, " % v for v in row) for row in spins]
+
+
 def write_equilibrate(model, lattice, n_samples_eq: int) -> str:
     K = model.K_
     N = lattice.N_
@@ -44,7 +49,7 @@ def write_equilibrate(model, lattice, n_samples_eq: int) -> str:
     for n in range(1, n_samples_eq + 1):
         if not write_iter(n):
             continue
-        lattice.sweep(n - done)
+        lattice.advance(n - done, getattr(model, "update_", "metropolis"))
         done = n
         sp = lattice.spins_
         NN = N * N
@@ -58,11 +63,9 @@ def write_equilibrate(model, lattice, n_samples_eq: int) -> str:
         lines.append("%d, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e, %10.7e" % (
             n, E / NN, E_sigma / NN, C_, M / NN, M_sigma / NN, Chi))
     if done < n_samples_eq:
-        lattice.sweep(n_samples_eq - done)
-    sp = lattice.spins_
+        lattice.advance(n_samples_eq - done, getattr(model, "update_", "metropolis"))
     lines.append("")
-    for i in range(N):
-        lines.append("# " + "".join("%d, " % v for v in sp[i]))
+    lines += spin_lines(lattice.spins_)
     with open(fn, "w") as f:
         f.write("\n".join(lines) + "\n")
     return fn

@@ -25,7 +25,7 @@ std::string rounded(double x, int precision) {
 }  // namespace
 
 Lattice::Lattice(int N, double K, uint64_t seed, uint32_t replica, int n_couplings, int device)
-    : N_(N), n_spins_(N * N), a_(1), spins_(N, N) {
+    : N_(N), n_spins_(N * N), a_(1), spins_(N, N), site_rng_(seed ^ ((uint64_t)replica << 32)) {
   mcrg_cfg cfg{};
   cfg.L = N;
   cfg.b = 2;
@@ -40,7 +40,7 @@ Lattice::Lattice(int N, double K, uint64_t seed, uint32_t replica, int n_couplin
 }
 
 Lattice::Lattice(int a, const SpinMatrix& spins, double K, uint64_t seed)
-    : N_(spins.rows()), n_spins_(spins.rows() * spins.rows()), a_(a), spins_(spins) {
+    : N_(spins.rows()), n_spins_(spins.rows() * spins.rows()), a_(a), spins_(spins), site_rng_(seed) {
   mcrg_cfg cfg{};
   cfg.L = N_;
   cfg.b = 2;
@@ -79,6 +79,44 @@ std::vector<double> Lattice::calc_interactions() {
 }
 
 double Lattice::calc_nearest_neighbor_interaction() { return calc_interactions()[0]; }
+
+void Lattice::write_spins(FILE* fptr) {
+  fprintf(fptr, "\n");
+  for (int i = 0; i < N_; ++i) {
+    fprintf(fptr, "# ");
+    for (int j = 0; j < N_; ++j) fprintf(fptr, "%i, ", spins_(i, j));
+    fprintf(fptr, "\n");
+  }
+}
+
+void Lattice::display_spins() {
+  for (int i = 0; i < N_; ++i) {
+    for (int j = 0; j < N_; ++j)
+      printf(spins_(i, j) == 1 ? "\033[34m%2s\033[0m" : "\033[37m%2s\033[0m", spins_(i, j) == 1 ? "O" : "X");
+    printf("\n");
+  }
+  printf("(Lattice spacing a = %i)\n\n", a_);
+}
+
+int Lattice::choose_random_spin() { return std::uniform_int_distribution<int>(0, n_spins_ - 1)(site_rng_); }
+
+SpinMatrix Lattice::nearest_neighbors(int i, int j) const {
+  const int N = N_;
+  auto w = [N](int x) { return (x % N + N) % N; };
+  SpinMatrix nn(4, 2);
+  const int r[4][2] = {{w(i + 1), j}, {w(i - 1), j}, {i, w(j + 1)}, {i, w(j - 1)}};
+  for (int k = 0; k < 4; ++k) nn(k, 0) = r[k][0], nn(k, 1) = r[k][1];
+  return nn;
+}
+
+SpinMatrix Lattice::next_nearest_neighbors(int i, int j) const {
+  const int N = N_;
+  auto w = [N](int x) { return (x % N + N) % N; };
+  SpinMatrix nnn(4, 2);
+  const int r[4][2] = {{w(i + 1), w(j + 1)}, {w(i - 1), w(j + 1)}, {w(i + 1), w(j - 1)}, {w(i - 1), w(j - 1)}};
+  for (int k = 0; k < 4; ++k) nnn(k, 0) = r[k][0], nnn(k, 1) = r[k][1];
+  return nnn;
+}
 
 IsingModel::IsingModel(double K) : K_(K), P_(1.0 - std::exp(2.0 * K)) {}
 
@@ -158,13 +196,7 @@ void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool 
     throw;
   }
   p->sync_spins();
-  // Lattice::write_spins (src/lattice.cpp:63-75)
-  fprintf(f, "\n");
-  for (int i = 0; i < p->N_; ++i) {
-    fprintf(f, "# ");
-    for (int j = 0; j < p->N_; ++j) fprintf(f, "%i, ", p->spins_(i, j));
-    fprintf(f, "\n");
-  }
+  p->write_spins(f);
   fclose(f);
 }
 

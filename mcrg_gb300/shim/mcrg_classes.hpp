@@ -20,7 +20,9 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -77,6 +79,20 @@ class Lattice {
   std::vector<double> calc_interactions();
   double calc_nearest_neighbor_interaction();
 
+  // src/lattice.cpp:63-75: "\n" then one "# s, s, ..., " line per row of the
+  // host mirror spins_
+  void write_spins(FILE* fptr);
+  // src/lattice.cpp:44-60: the mirror as coloured O (+1) / X (-1) on stdout
+  void display_spins();
+  // src/lattice.cpp:78-81: a uniform site index in [0, N^2) from the
+  // lattice's own mt19937_64 (seeded from seed and replica)
+  int choose_random_spin();
+  // src/lattice.cpp:124-151: periodic neighbours of (i, j) as a 4 x 2 matrix
+  // of (row, column): (i+1, j), (i-1, j), (i, j+1), (i, j-1) and diagonals
+  // (i+1, j+1), (i-1, j+1), (i+1, j-1), (i-1, j-1)
+  SpinMatrix nearest_neighbors(int i, int j) const;
+  SpinMatrix next_nearest_neighbors(int i, int j) const;
+
   // push host edits of spins_ to the device / pull the device state
   void upload_spins();
   void sync_spins();
@@ -92,6 +108,7 @@ class Lattice {
 
  private:
   mcrg_ctx* ctx_ = nullptr;
+  std::mt19937_64 site_rng_;
 };
 
 // Update rule of a Monte Carlo step: a checkerboard Metropolis sweep, or a

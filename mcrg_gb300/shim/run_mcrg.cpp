@@ -4,8 +4,11 @@
 //        run_mcrg locate L n_iterations n_eq n_samples K0 [seed]
 //          (MonteCarloRenormalizationGroup::locate_critical_point)
 //        run_mcrg rgnn N seed W00 W01 W10 W11  (Lattice::rgnn_scalar_output of the initial coin)
-//        run_mcrg equilibrate N n K [seed]
+//        run_mcrg equilibrate N n K [seed] [metropolis|wolff|sw]
 //          (IsingModel::equilibrate(lattice, n, true): writes equilibrate_N_*.txt)
+//        run_mcrg lattice N seed n_draws
+//          (the Lattice members: neighbour tables, write_spins, display_spins,
+//           choose_random_spin, Lattice(a, spins))
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
@@ -30,10 +33,48 @@ int main(int argc, char** argv) {
     const int n = argc > 3 ? atoi(argv[3]) : 1000;
     const double K = argc > 4 ? atof(argv[4]) : -0.44068679350977147;
     const uint64_t seed = argc > 5 ? strtoull(argv[5], nullptr, 10) : 1;
+    const std::string u = argc > 6 ? argv[6] : "metropolis";
     try {
       std::shared_ptr<Lattice> lat(new Lattice(N, K, seed));
       IsingModel model(K);
+      model.update_ = u == "wolff" ? Update::Wolff : u == "sw" ? Update::SwendsenWang : Update::Metropolis;
       model.equilibrate(lat, n, true);
+    } catch (const McrgError& e) {
+      fprintf(stderr, "error: %s\n", e.what());
+      return 1;
+    }
+    return 0;
+  }
+  if (argc > 4 && std::string(argv[1]) == "lattice") {
+    const int N = atoi(argv[2]);
+    const uint64_t seed = strtoull(argv[3], nullptr, 10);
+    const int n_draws = atoi(argv[4]);
+    try {
+      Lattice lat(N, -0.44068679350977147, seed);
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+          const SpinMatrix nn = lat.nearest_neighbors(i, j), nnn = lat.next_nearest_neighbors(i, j);
+          printf("NB %d %d", i, j);
+          for (int k = 0; k < 4; ++k) printf(" %d %d", nn(k, 0), nn(k, 1));
+          for (int k = 0; k < 4; ++k) printf(" %d %d", nnn(k, 0), nnn(k, 1));
+          printf("\n");
+        }
+      printf("DRAWS");
+      for (int k = 0; k < n_draws; ++k) printf(" %d", lat.choose_random_spin());
+      printf("\nSPINS");
+      fflush(stdout);
+      lat.write_spins(stdout);
+      printf("DISPLAY\n");
+      lat.display_spins();
+      // Lattice(a, spins): the mirror flipped, spacing 2
+      SpinMatrix flipped(N, N);
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) flipped(i, j) = -lat.spins_(i, j);
+      Lattice lat2(2, flipped);
+      lat2.sync_spins();
+      printf("A2 %d SNN %.0f SNN2 %.0f\nFLIPPED", lat2.a_, lat.calc_nearest_neighbor_interaction(),
+             lat2.calc_nearest_neighbor_interaction());
+      lat2.write_spins(stdout);
     } catch (const McrgError& e) {
       fprintf(stderr, "error: %s\n", e.what());
       return 1;
