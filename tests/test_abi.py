@@ -57,3 +57,33 @@ def test_argument_validation_without_gpu(mcrg_lib):
         assert mcrg_lib.mcrg_alloc(ctypes.byref(h), ctypes.byref(cfg)) == _abi.EINVAL
     assert mcrg_lib.mcrg_sweep(None, 1) == _abi.EINVAL
     assert mcrg_lib.mcrg_free(None) == _abi.EINVAL
+
+
+def test_null_handles_and_bad_arguments_rejected(mcrg_lib):
+    """Every entry point rejects a NULL handle or an out-of-range argument with an
+    error code before it touches the GPU or dereferences a pointer (the reference has
+    no error path; its classes would crash or read out of bounds instead)."""
+    import numpy as np
+    from mcrg_gb300 import _abi
+    C, N, E = ctypes, None, _abi.EINVAL
+    lib = mcrg_lib
+    buf = np.zeros(2048 * 2048, dtype=np.int8)
+    bp = buf.ctypes.data_as(ctypes.c_void_p)
+    out = (C.c_int64 * 8)()
+    for rc in (lib.mcrg_set_spins(N, N), lib.mcrg_get_spins(N, N), lib.mcrg_sweep(N, 1), lib.mcrg_block(N, 1, N),
+               lib.mcrg_interactions(N, N), lib.mcrg_measure(N, 1, 1, N, 0, N, 0),
+               lib.mcrg_rgnn_scalar_output(N, N, N), lib.mcrg_measure_flow(N, 1, 1, N),
+               lib.mcrg_cluster_update(N, 1, 1, N), lib.mcrg_measure_cluster(N, 1, 1, 1, N, 0, N, 0),
+               lib.mcrg_counters(N, N, N), lib.mcrg_set_counters(N, 0, 0), lib.mcrg_tile_shape(N, N, N),
+               lib.mcrg_stream(N, N), lib.mcrg_sync(N),
+               lib.mcrg_alloc(N, C.byref(_abi.Cfg(64, 2, -1, 2, -0.44, 1, 0, 0))),
+               lib.mcrg_alloc(C.byref(C.c_void_p()), N),
+               lib.mcrg_alloc(C.byref(C.c_void_p()), C.byref(_abi.Cfg(64, 2, -1, 2, float("nan"), 1, 0, 0))),
+               lib.mcrg_server_create(N, N), lib.mcrg_submit(N, N, N), lib.mcrg_poll(N, 1, N),
+               lib.mcrg_cancel(N, 1), lib.mcrg_wait(N, 1, 0.0, N), lib.mcrg_server_stats(N, N, N, N, N),
+               lib.mcrg_server_destroy(N), lib.mcrg_batch_run(N, 1, N, 0, 0), lib.mcrg_batch_run(N, -1, N, 0, 0),
+               lib.mcrg_block_lattice(6, bp, N, 1, 0, 1, 0, bp, 0), lib.mcrg_block_lattice(8, N, N, 1, 0, 1, 0, bp, 0),
+               lib.mcrg_lattice_couplings(8, bp, 7, out, 0), lib.mcrg_lattice_couplings(8, N, 2, out, 0),
+               lib.mcrg_lattice_couplings_noalloc(8, N, 2, out, 0)):
+        assert rc == E
+    assert lib.mcrg_lattice_couplings_noalloc(2048, bp, 2, out, 0) == _abi.ENOSPC
