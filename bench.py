@@ -525,6 +525,32 @@ def cpu_reference(L: int, seconds: float, threads: int, n_couplings: int = 2) ->
         ref.close()
 
 
+def cpu_checkerboard(seconds: float, threads: int, L: int = 1024) -> dict:
+    """The like-for-like host flip rate: the oracle's Philox checkerboard sweep
+    (the same update the GPU runs, one scalar site at a time) on `threads`
+    independent L x L lattices, one OS thread each (ctypes releases the GIL)."""
+    from oracle import oracle as O
+    lib = O.lib()
+    lats = [O.init_spins(L, 1, k) for k in range(threads)]
+    done = [0] * threads
+
+    def work(k):
+        p = C.c_void_p(lats[k].ctypes.data)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            lib.orc_sweep(L, p, KC, 1, k, done[k], 1)
+            done[k] += 1
+
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    return {"flips_per_s": sum(done) * L * L / wall, "sweeps": sum(done), "wall_s": wall, "L": L}
+
+
 def cpu_threads(L: int) -> int:
     """All host threads, capped at 8 for L >= 8192 (each Wolff replica holds
     ~2.3 GB of host state at L = 16384)."""
@@ -598,6 +624,12 @@ def main():
                                "sample": "reference Wolff update + measurement, %d independent replicas on %d "
                                          "threads for %.1f s (%d samples)" % (threads, threads, cb["wall_s"],
                                                                              cb["samples"])}
+        ck_threads = os.cpu_count() or 1
+        ck = cpu_checkerboard(min(5.0, args.cpu_seconds / 3), ck_threads)
+        out["cpu_baseline"]["checkerboard_port"] = {
+            "value": round(ck["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": ck_threads,
+            "sample": "oracle Philox checkerboard sweeps, %d independent L=%d lattices on %d threads for %.1f s "
+                      "(%d sweeps)" % (ck_threads, ck["L"], ck_threads, ck["wall_s"], ck["sweeps"])}
     if D.rank == 0:
         print(json.dumps(out), flush=True)
 
