@@ -83,7 +83,7 @@ enum {
   MCRG_EBUSY = -16,      /* server queue full */
   MCRG_EINVAL = -22,     /* bad argument */
   MCRG_ENOSPC = -28,     /* request exceeds the memory budget */
-  MCRG_ENOSYS = -38,     /* not supported by this build */
+  MCRG_ENOSYS = -38,     /* operation not supported for this configuration */
   MCRG_ETIMEDOUT = -110, /* bounded wait ran out */
   MCRG_ECANCELED = -125  /* request cancelled / server shut down */
 };

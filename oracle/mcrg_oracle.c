@@ -1,7 +1,7 @@
 /*
  * mcrg_oracle.c -- CPU oracle for the MCRG Monte-Carlo / block-spin hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: only tests/,
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs may
  * load it.  The product (libmcrg, the CUDA path) never links or calls it.
  *

@@ -2,7 +2,7 @@
 
 Golden vectors come from kim-jane/MCRG compiled unmodified
 (tests/golden/make_golden.py); these tests prove the C restatement
-(oracle/mcrg_oracle.c) reproduces them before it is trusted as the checker.
+(oracle/mcrg_oracle.c) reproduces them before it is trusted as the oracle.
 """
 import math
 
