@@ -234,7 +234,21 @@ int mcrg_set_counters(mcrg_ctx* ctx, uint64_t sweeps, uint64_t samples);
 int mcrg_tile_shape(mcrg_ctx* ctx, int32_t* tile_rows, int32_t* tile_cols);
 /* The context's CUDA stream (cudaStream_t), for event timing. */
 int mcrg_stream(mcrg_ctx* ctx, void** stream);
+/* Drains the context's stream.  Like every entry point that returns results
+ * (mcrg_get_spins, mcrg_block, mcrg_interactions, mcrg_measure*), it returns
+ * MCRG_ETIMEDOUT when an HBM sweep since the last such call gave up waiting
+ * for a bulk copy of its band (bounded wait of 1 s; the lattice is then not
+ * a valid chain state), and clears that flag. */
 int mcrg_sync(mcrg_ctx* ctx);
+
+/* Self-test of the bounded device waits, without a fault: one kernel on
+ * `device` waits with the library's bounded wait on a barrier that nothing
+ * completes, for limit_us (1 .. 1e6) microseconds.  Returns MCRG_OK when the
+ * kernel ran and the device stays usable, with *status = MCRG_ETIMEDOUT (the
+ * wait ran out and raised the error flag, the expected outcome) and
+ * *waited_s = the device time the wait took.  No counterpart in the
+ * reference. */
+int mcrg_selftest_wait(int32_t device, int64_t limit_us, int32_t* status, double* waited_s);
 
 /* Stateless device forms of block_spin_transformation (src/mcrg.cpp:314-348)
  * and calc_interactions (src/lattice.cpp:102-120) on a host lattice.

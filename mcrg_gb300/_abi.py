@@ -92,6 +92,7 @@ _SIGS = {
     "mcrg_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
     "mcrg_tile_shape": (C.c_int, [C.c_void_p, P(C.c_int32), P(C.c_int32)]),
     "mcrg_sync": (C.c_int, [C.c_void_p]),
+    "mcrg_selftest_wait": (C.c_int, [C.c_int32, C.c_int64, P(C.c_int32), P(C.c_double)]),
     "mcrg_block_lattice": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_int32,
                                      C.c_uint32, C.c_void_p, C.c_int32]),
     "mcrg_lattice_couplings": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, P(C.c_int64), C.c_int32]),

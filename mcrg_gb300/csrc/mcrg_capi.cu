@@ -15,6 +15,7 @@
 
 #include "mcrg_internal.cuh"
 #include "mcrg_tiled.cuh"
+#include "mcrg_tma.cuh"
 
 using namespace mcrg;
 
@@ -226,6 +227,23 @@ int run_resident(mcrg_ctx* c, int64_t n_eq, int64_t n_samples, int64_t sweeps_be
   return MCRG_OK;
 }
 
+// One thread waits, with the kernels' bounded wait, on an mbarrier that
+// nothing arrives at: the wait runs out after limit_ns and raises the flag.
+// No copy is ever issued on the barrier, so the block can leave it pending.
+__global__ void wait_selftest_kernel(uint64_t limit_ns, int* status, unsigned long long* waited_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = tma::globaltimer_ns();
+    if (!tma::mbar_wait_bounded(&bar, 0u, limit_ns)) atomicOr(status, 1);
+    *waited_ns = tma::globaltimer_ns() - t0;
+  }
+}
+
 }  // namespace
 
 namespace mcrg {
@@ -387,6 +405,16 @@ int mcrg_set_spins(mcrg_ctx* c, const int8_t* host) {
   return bad ? MCRG_EINVAL : MCRG_OK;
 }
 
+// The HBM sweep kernel raises a flag when a bulk copy of its band does not
+// land within its bounded wait (the lattice it wrote is then not a valid
+// sweep).  Entry points that return results drain the stream, read and clear
+// the flag, and report MCRG_ETIMEDOUT instead of the results.
+static int sweep_status(mcrg_ctx* c) {
+  if (!c->is_tiled) return MCRG_OK;
+  const int h = tiled_status(&c->tiled, c->stream);
+  return h < 0 ? MCRG_EIO : h ? MCRG_ETIMEDOUT : MCRG_OK;
+}
+
 int mcrg_get_spins(mcrg_ctx* c, int8_t* host) {
   if (!c || !host) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
@@ -402,7 +430,7 @@ int mcrg_get_spins(mcrg_ctx* c, int8_t* host) {
   CK(cudaGetLastError());
   if (!direct) CK(cudaMemcpyAsync(host, c->d_nat, (size_t)L * L, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  return MCRG_OK;
+  return sweep_status(c);
 }
 
 int mcrg_sweep(mcrg_ctx* c, int64_t n_sweeps) {
@@ -461,6 +489,7 @@ static int measure_impl(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, 
                        c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
+  if (int rc = sweep_status(c)) return rc;
   for (int64_t q = 0; q < nb; ++q) {
     if (total) add_moments(total, &h[(size_t)q]);
     if (bins && q < n_bins_cap) bins[q] = h[(size_t)q];
@@ -644,6 +673,7 @@ int mcrg_block(mcrg_ctx* c, int level, int8_t* host_out) {
       rc = MCRG_EIO;
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
+  if (!rc) rc = sweep_status(c);
   cudaFree(tmp);
   return rc;
 }
@@ -683,6 +713,7 @@ int mcrg_interactions(mcrg_ctx* c, int64_t* out) {
   int hS[(MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS];
   if (!rc && cudaMemcpyAsync(hS, dS, sizeof hS, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = MCRG_EIO;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
+  if (!rc) rc = sweep_status(c);
   cudaFree(tmp);
   cudaFree(dS);
   if (rc) return rc;
@@ -723,7 +754,33 @@ int mcrg_stream(mcrg_ctx* c, void** stream) {
 int mcrg_sync(mcrg_ctx* c) {
   if (!c) return MCRG_EINVAL;
   CK(cudaSetDevice(c->cfg.device));
-  return to_status(cudaStreamSynchronize(c->stream));
+  const int rc = to_status(cudaStreamSynchronize(c->stream));
+  return rc ? rc : sweep_status(c);
+}
+
+int mcrg_selftest_wait(int32_t device, int64_t limit_us, int32_t* status, double* waited_s) {
+  if (!status || limit_us < 1 || limit_us > 1000000) return MCRG_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return MCRG_EIO;
+  CK(cudaSetDevice(device));
+  struct {
+    int flag;
+    int pad;
+    unsigned long long waited;
+  } h{}, *d = nullptr;
+  CK(cudaMalloc(&d, sizeof h));
+  int rc = MCRG_OK;
+  if (cudaMemset(d, 0, sizeof h) != cudaSuccess) rc = MCRG_EIO;
+  if (!rc) {
+    wait_selftest_kernel<<<1, 32>>>((uint64_t)limit_us * 1000ull, &d->flag, &d->waited);
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = MCRG_EIO;
+  }
+  cudaFree(d);
+  if (rc) return rc;
+  *status = h.flag ? MCRG_ETIMEDOUT : MCRG_OK;
+  if (waited_s) *waited_s = (double)h.waited * 1e-9;
+  return MCRG_OK;
 }
 
 int mcrg_block_lattice(int32_t N, const int8_t* host_in, const int8_t* tie_values, uint64_t seed, uint32_t replica,

@@ -411,6 +411,9 @@ int tiled_status(TiledLattice* t, cudaStream_t s) {
   int h = 0;
   if (cudaMemcpyAsync(&h, t->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
   if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  if (h != 0 && (cudaMemsetAsync(t->d_status, 0, sizeof(int), s) != cudaSuccess ||
+                 cudaStreamSynchronize(s) != cudaSuccess))
+    return -1;
   return h;
 }
 

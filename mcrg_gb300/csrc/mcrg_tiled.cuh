@@ -43,7 +43,9 @@ int tiled_measure_sample(TiledLattice* t, uint32_t sample, mcrg_moments* bin, cu
 // Sweep schedule in use (after the first sweep): rows per pipeline group
 // and threads per CTA; returns the variant index.
 int tiled_variant(TiledLattice* t, int* rows, int* threads);
-// Device error flags raised by the tiled kernels (0 = none).
+// Drains the stream and returns the sweep kernel's error flags since the
+// last call (1 = a bulk copy did not land within the bounded wait), clearing
+// them; -1 when the stream itself failed.
 int tiled_status(TiledLattice* t, cudaStream_t s);
 
 }  // namespace mcrg

@@ -28,11 +28,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Longest a kernel waits for a bulk copy before it reports an error.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s
+
 // Waits for phase `parity` of `bar` to complete; gives up (false) after
-// 2^24 polls so that a lost copy turns into an error flag, not a hang.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 24); ++it)
+// limit_ns of device time or 2^24 polls, whichever comes first, so that a
+// lost copy turns into an error flag, not a hang.  The clock is read only
+// once the first poll has failed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t limit_ns = kWaitLimitNs) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  }
   return false;
 }
 

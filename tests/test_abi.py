@@ -84,6 +84,8 @@ def test_null_handles_and_bad_arguments_rejected(mcrg_lib):
                lib.mcrg_server_destroy(N), lib.mcrg_batch_run(N, 1, N, 0, 0), lib.mcrg_batch_run(N, -1, N, 0, 0),
                lib.mcrg_block_lattice(6, bp, N, 1, 0, 1, 0, bp, 0), lib.mcrg_block_lattice(8, N, N, 1, 0, 1, 0, bp, 0),
                lib.mcrg_lattice_couplings(8, bp, 7, out, 0), lib.mcrg_lattice_couplings(8, N, 2, out, 0),
-               lib.mcrg_lattice_couplings_noalloc(8, N, 2, out, 0)):
+               lib.mcrg_lattice_couplings_noalloc(8, N, 2, out, 0),
+               lib.mcrg_selftest_wait(0, 1000, N, N), lib.mcrg_selftest_wait(0, 0, C.byref(C.c_int32()), N),
+               lib.mcrg_selftest_wait(0, 1000001, C.byref(C.c_int32()), N)):
         assert rc == E
     assert lib.mcrg_lattice_couplings_noalloc(2048, bp, 2, out, 0) == _abi.ENOSPC
