@@ -262,6 +262,11 @@ __global__ void __launch_bounds__(NT, MINB)
   if (tid < 6) qn[tid] = 0;
   if (tid == 0) tma::fence_mbar_init();
   __syncthreads();
+  // Launched as a programmatic dependent of the previous sweep: its output is
+  // this launch's input and its input this launch's output, so every thread
+  // waits for it before the first copy or store.
+  tma::griddep_wait();
+  tma::griddep_launch_dependents();
   if (tid < 32)
     for (int g = 0; g < LEAD && g < J; ++g) issue_group<NS, LW, LEAD>(g, top, b0, b1, ms, in, raw, bar, lane);
 

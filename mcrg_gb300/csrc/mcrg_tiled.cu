@@ -194,7 +194,19 @@ void launch_variant(const TiledLattice* t, int vi, const uint8_t* in, uint8_t* o
   if (bands > v.waves * t->sms * per_sm) bands = v.waves * t->sms * per_sm;
   if (bands < 1) bands = 1;
   void* args[] = {(void*)&in, (void*)&out, (void*)&P, (void*)&tt, (void*)&t->d_status};
-  cudaLaunchKernel(v.kern, dim3(bands), dim3(block_threads(v)), args, v.smem, s);
+  // programmatic dependent launch: the CTAs of this sweep are scheduled while
+  // the previous kernel drains and wait for it inside the kernel
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(bands);
+  cfg.blockDim = dim3(block_threads(v));
+  cfg.dynamicSmemBytes = v.smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelExC(&cfg, v.kern, args);
 }
 
 int first_tail_level(int L) {

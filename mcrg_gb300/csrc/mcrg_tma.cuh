@@ -61,6 +61,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// Programmatic dependent launch: griddep_wait() returns once the grids this
+// launch depends on (the previous kernel on the stream) have completed and
+// their memory is visible (at once for a launch without the attribute);
+// griddep_launch_dependents() lets the next launch be scheduled before this
+// grid ends, so its prologue overlaps this grid's tail.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // Orders this thread's earlier shared-memory accesses before later bulk copies.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
