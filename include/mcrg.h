@@ -148,10 +148,12 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg);
 int mcrg_free(mcrg_ctx* ctx);
 
 /* Replaces writes / reads of the public Lattice::spins_ (src/lattice.hpp:16;
- * read directly by src/rgnn.cpp:113-114,175).  Values must be +-1.  A
- * page-locked, 16-byte-aligned host buffer (L >= 32) is read / written in
- * place by the layout-conversion kernel over the host link; other buffers go
- * through a staging copy.  Both return after the transfer completed. */
+ * read directly by src/rgnn.cpp:113-114,175).  Values must be +-1.
+ * mcrg_set_spins reads a page-locked, 16-byte-aligned host buffer (L >= 32)
+ * in place with the layout-conversion kernel over the host link; other
+ * buffers go through a staging copy.  mcrg_get_spins converts on the device
+ * and copies the rows out with one transfer (at host-link speed when the
+ * buffer is page-locked).  Both return after the transfer completed. */
 int mcrg_set_spins(mcrg_ctx* ctx, const int8_t* host_spins);
 int mcrg_get_spins(mcrg_ctx* ctx, int8_t* host_spins);
 
