@@ -257,11 +257,15 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
     const int vi = (v >> lg) - i0, vj = (v & (L - 1)) - j0;
     return ((unsigned)vi < 32u && (unsigned)vj < 32u) ? (vi << 5) + vj : -1;
   };
+  // Every site resolves through one entry of the list: its label's site when
+  // that lies in the tile (a member's in-tile root, or the root another
+  // in-tile root was linked to), else itself (a root the merge linked to
+  // another tile).
   for (int x = threadIdx.x; x < 1024; x += 256) {
     const int v = label[((size_t)(i0 + (x >> 5)) << lg) + j0 + (x & 31)];
     lbl[x] = v;
     const int q = loc(v);
-    if (q >= 0) need[q] = 1;
+    need[q >= 0 ? q : x] = 1;
   }
   __syncthreads();
   // the in-tile components' roots as a dense list (one shared atomic per warp and pass), so that
@@ -286,15 +290,8 @@ __global__ void __launch_bounds__(256) cl_flip32_kernel(uint8_t* __restrict__ st
   const int h = L / 2;
   unsigned cnt = 0;
   for (int r = warp; r < 32; r += 8) {
-    const int v = lbl[(r << 5) + lane], q = loc(v);
-    bool flip;
-    if (q >= 0) {
-      flip = wolff ? groot[q] == seed_root : coin[q] != 0;
-    } else {  // a tile root the merge linked elsewhere: its own root
-      const int g = find_halve(label, v, err);
-      flip = wolff ? g == seed_root
-                   : (stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)g >> 16, (uint32_t)g & 0xFFFFu, t).x & 1u) != 0;
-    }
+    const int x = (r << 5) + lane, q = loc(lbl[x]), k = q >= 0 ? q : x;
+    const bool flip = wolff ? groot[k] == seed_root : coin[k] != 0;
     const uint32_t m = __ballot_sync(0xFFFFFFFFu, flip);
     if (lane < 2 && m) {  // lane c: the 16 bytes of colour c in this row segment
       const int i = i0 + r, c = lane, par = (i + c) & 1;  // colour c holds the columns of parity (i + c) & 1
