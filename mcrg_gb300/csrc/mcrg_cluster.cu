@@ -150,9 +150,11 @@ __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restric
   __shared__ int par[1024];
   __shared__ uint8_t sp[33 * 32];  // spins of the tile's rows and of the row below it
   __shared__ uint32_t hb[32], vb[32];
+  __shared__ int vlist[1024], nv;  // vertical bonds that join two runs, as their upper site
   const int tpr = L >> 5, ti = blockIdx.x / tpr, tj = blockIdx.x - ti * tpr;
   const int i0 = ti << 5, j0 = tj << 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool one = L == 32;  // a one-tile lattice: its wrap bonds are in-tile bonds
+  if (threadIdx.x == 0) nv = 0;
   if (threadIdx.x < 66) {  // 33 rows x 2 colours: 16 bytes each, de-interleaved into natural order
     const int r = threadIdx.x >> 1, c = threadIdx.x & 1, i = (i0 + r) & (L - 1), h = L / 2;
     const uint4 v = *reinterpret_cast<const uint4*>(st + (size_t)c * L * h + (size_t)i * h + (j0 >> 1));
@@ -185,13 +187,25 @@ __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restric
     }
   }
   __syncthreads();
+  // The unions go through one list for the whole tile, so that the rows with
+  // the longest union chains do not hold every other warp at the barrier.
   for (int r = warp; r < 32; r += 8) {
     const int rn = (r + 1) & 31;
     const uint32_t v = vb[r], hr = hb[r], hn = hb[rn];
     const uint32_t dup = (v & hr & hn) << 1;  // column c-1 already joins the same two runs
-    if (((v & ~dup) >> lane) & 1u) unite<true>(par, r * 32 + lane, rn * 32 + lane, err);
-    if (one && lane == 31 && (hr >> 31)) unite<true>(par, r * 32 + 31, r * 32, err);  // horizontal wrap
+    const uint32_t m = v & ~dup;
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&nv, __popc(m));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if ((m >> lane) & 1u) vlist[base + __popc(m & ((1u << lane) - 1u))] = r * 32 + lane;
   }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nv; e += 256) {
+    const int x = vlist[e];
+    unite<true>(par, x, (x + 32) & 1023, err);
+  }
+  if (one && threadIdx.x < 32 && (hb[threadIdx.x] >> 31))  // horizontal wrap of a one-tile lattice
+    unite<true>(par, threadIdx.x * 32 + 31, threadIdx.x * 32, err);
   __syncthreads();
   for (int x = threadIdx.x; x < 1024; x += 256) {
     const int r = find_root(par, x, err);
