@@ -420,6 +420,23 @@ def test_full_size_lattice_one_sweep(M, monkeypatch):
         del got
 
 
+def test_full_size_chain_and_measurement(M):
+    """The benchmark's own path at its size: L = 16384, 13 levels, 5 couplings, the
+    autotuned sweep launched back to back (each sweep a programmatic dependent of the
+    previous one), two measurements two sweeps apart; moments and final spins bit-exact
+    against the oracle's chain."""
+    N, C, seed, rep = 16384, 5, 21, 1
+    nl = int(math.log2(N)) - 1
+    lat = M.Lattice(N, KC, seed=seed, replica=rep, n_couplings=C)
+    lat.sweep(3)
+    tot, _ = lat.measure(2, 2)
+    trace, fin = O.chain(N, KC, C, nl, seed, rep, n_eq=3, n_samples=2, sweeps_between=2)
+    assert_moments_equal(tot, MomentSums.from_trace(trace))
+    got = lat.spins_
+    lat.close()
+    assert np.array_equal(got, fin), "final spins differ at %d sites" % int((got != fin).sum())
+
+
 # --------------------------------------------------------------------------
 # checkpoint / resume and request cancellation
 # --------------------------------------------------------------------------
