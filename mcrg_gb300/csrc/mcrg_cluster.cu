@@ -14,7 +14,8 @@
 //      natural index i*L + j of its in-tile component.  With T = 32 a warp
 //      owns a tile row: the row's open horizontal bonds form a ballot mask,
 //      every site points at the first site of its run (count leading zeros),
-//      and only vertical bonds are united, one per pair of runs;
+//      and only vertical bonds are united, one per pair of runs, taken by
+//      all threads from one list for the whole tile;
 //   2. cl_merge_kernel (L > 32): every open bond that crosses a tile edge
 //      unites the two trees of the global forest; atomicMin links the larger
 //      root under the smaller, so a root is always the smallest index of its
@@ -23,7 +24,9 @@
 //   3. cl_flip_kernel: every site finds its root; Wolff flips the sites that
 //      share the seed's root, Swendsen-Wang the sites whose root draws a set
 //      bit; the flips are counted.  With T = 32 a CTA loads its tile's labels
-//      and resolves the global root (and coin) once per in-tile component.
+//      and resolves the global root (and coin) once per entry of a compacted
+//      list: each in-tile component's root, and each tile root the merge
+//      linked into another tile.
 // The result depends only on the bond draws, never on the order in which
 // threads unite, so it is reproducible and equal to the oracle's labelling.
 // Union and find loops make progress by construction (labels only decrease);
