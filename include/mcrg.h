@@ -269,13 +269,15 @@ int mcrg_lattice_couplings(int32_t N, const int8_t* host_in, int32_t n_couplings
  * working copy lives in a fixed scratch array that is part of libmcrg.so and
  * stays reserved on every GPU that loads the library until the process ends
  * (2 * MCRG_NOALLOC_MAX_L^2 + 256 bytes).  N above MCRG_NOALLOC_MAX_L is
- * rejected with MCRG_ENOSPC.  The first call on a device looks the array's
- * address up for that device; make that first call before any stream
- * capture.  All calls share the array and it keeps the last call's data; the
- * sums are cleared at the start of each call.  Calls on one device are
- * serialised by a lock inside the library; device work that overlaps with a
- * call in any other way races on the array.  No counterpart in the
- * reference. */
+ * rejected with MCRG_ENOSPC.  The first call on a device sets it up: it
+ * looks the array's address up for that device and creates the one
+ * non-blocking stream all calls on the device use (so a call neither uses the
+ * legacy default stream nor waits for the caller's streams); make that first
+ * call before any stream capture.  All calls share the array and it keeps
+ * the last call's data; the sums are cleared at the start of each call.
+ * Calls on one device are serialised by a lock inside the library, held until
+ * the call's device work is done; device work that overlaps with a call in
+ * any other way races on the array.  No counterpart in the reference. */
 #define MCRG_NOALLOC_MAX_L 1024
 int mcrg_lattice_couplings_noalloc(int32_t N, const int8_t* host_in, int32_t n_couplings, int64_t* out,
                                    int32_t device);

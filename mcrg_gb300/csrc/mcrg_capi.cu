@@ -247,6 +247,11 @@ __global__ void wait_selftest_kernel(uint64_t limit_ns, int* status, unsigned lo
 }  // namespace
 
 namespace mcrg {
+cudaError_t launch_nat_to_split(const int8_t* d_nat, int N, uint8_t* d_split, int* d_bad, cudaStream_t s) {
+  void* args[] = {(void*)&d_nat, (void*)&N, (void*)&d_split, (void*)&d_bad};
+  return cudaLaunchKernel((const void*)nat_to_split_kernel, dim3(grid_for((int64_t)N * N)), dim3(256), args, 0, s);
+}
+
 Accept make_accept(double K) {
   Accept a;
   memset(&a, 0, sizeof a);

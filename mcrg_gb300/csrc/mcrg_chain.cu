@@ -265,8 +265,8 @@ cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out,
   int blocks = (work + 255) / 256;
   if (blocks < 1) blocks = 1;
   if (blocks > 4096) blocks = 4096;
-  couplings_once_kernel<<<blocks, 256, 0, s>>>(d_in, N, C, d_out);
-  return cudaGetLastError();
+  void* args[] = {(void*)&d_in, (void*)&N, (void*)&C, (void*)&d_out};
+  return cudaLaunchKernel((const void*)couplings_once_kernel, dim3(blocks), dim3(256), args, 0, s);
 }
 
 }  // namespace mcrg

@@ -112,6 +112,9 @@ cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels
 cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat,
                               Key key, uint32_t replica, int level, uint32_t sample, cudaStream_t s);
 cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out, cudaStream_t s);
+// Natural-layout int8 +-1 lattice -> split layout; *d_bad |= 1 on a value
+// other than +-1.  Returns the launch's own status (no cudaGetLastError).
+cudaError_t launch_nat_to_split(const int8_t* d_nat, int N, uint8_t* d_split, int* d_bad, cudaStream_t s);
 
 // One cluster update (Wolff or Swendsen-Wang, mcrg_cluster.cu) of a split-
 // layout lattice of side L at update index t: d_label holds L^2 ints,

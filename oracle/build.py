@@ -5,7 +5,8 @@
   on x86-64 and aarch64).
 * ``build_ref()`` compiles the reference's own unmodified sources
   (src/definitions.cpp, lattice.cpp, ising.cpp, mcrg.cpp, rgnn.cpp of kim-jane/MCRG,
-  read where they lie under ``/root/reference``) together with
+  read where they lie under the reference checkout: ``$MCRG_REFERENCE_DIR``,
+  by default ``/root/reference``) together with
   ``oracle/ref_harness.cpp`` and the single-rank ``oracle/stub_mpi/mpi.h``
   into ``oracle/_ref/libmcrg_ref.so``.  Nothing is copied out of the
   reference tree.  Only possible where the reference is mounted.
@@ -17,7 +18,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/src"
+REF_ROOT = os.environ.get("MCRG_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmcrg_ref.so")
 

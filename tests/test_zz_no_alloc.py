@@ -40,6 +40,24 @@ def test_noalloc_matches_allocating_entry_point_twice(mcrg_lib, N):
     np.testing.assert_array_equal(got, _existing(mcrg_lib, small, 2))
 
 
+def test_noalloc_allocates_no_device_memory(mcrg_lib):
+    """The property the call exists for: after a warm-up call (which sets the
+    device up), further calls leave the device's free memory unchanged."""
+    import torch
+    rng = np.random.default_rng(7)
+    s = np.where(rng.random((1024, 1024)) < 0.5, 1, -1).astype(np.int8)
+    rc, want = _noalloc(mcrg_lib, s)
+    assert rc == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(5):
+        rc, got = _noalloc(mcrg_lib, s)
+        assert rc == 0
+        np.testing.assert_array_equal(got, want)
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+
+
 def test_noalloc_rejects_oversize_and_bad_input(mcrg_lib):
     from mcrg_gb300 import _abi
     big = np.ones((2048, 2048), dtype=np.int8)
