@@ -311,11 +311,37 @@ typedef struct {
   mcrg_moments moments;
 } mcrg_result;
 
-/* Runs every request in one persistent launch on `device` (CUDA-graph
- * captured when `use_graph` != 0) and fills results[i].  Lattices above
- * MCRG_SMEM_MAX_L run on the tiled HBM path after the resident batch. */
+/* Runs a batch of independent chains on `device` and fills results[i]
+ * (the GPU form of the reference's one chain per MPI rank + MPI_Allreduce,
+ * src/mcrg.cpp:42,101-103).  Every request that fits a shared-memory-
+ * resident chain (fast acceptance regime up to MCRG_RESIDENT_MAX_L; other K
+ * up to MCRG_SMEM_MAX_L; cluster updates up to 256) runs in ONE persistent
+ * launch: the chains are grouped into packs (one chain per warp-aligned
+ * group of a CTA's threads), ordered longest first, and the CTAs take packs
+ * from a queue until it is empty.  The threads per chain of each shape
+ * (side, chain form, levels, couplings) are picked once per process by the
+ * schedule autotuner from timed trial launches (mcrg_batch_schedule); for
+ * resident sides above MCRG_SMEM_MAX_L it also times the tiled HBM path and
+ * runs those requests there when that ends sooner.  With `use_graph` != 0
+ * the upload, clear, launch and download are one CUDA graph, instantiated
+ * once per device, CTA width, grid and buffer set and re-launched with
+ * updated copy sizes.  Requests that no chain holds run on the tiled HBM
+ * path after the resident launch.  Environment: MCRG_POOL_THREADS=<n>
+ * forces n threads per chain where n is a candidate; MCRG_BATCH_SCHEDULE=
+ * resident | tiled forces the choice for the largest resident sides. */
 int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* results, int32_t device,
                    int32_t use_graph);
+
+/* The schedule the autotuner picked (tuning it now if needed) for chains of
+ * the request's shape: threads per chain, seconds per sample of one chain in
+ * a full wave of the trial, and seconds per sample of the tiled HBM path
+ * (-1 when not timed).  MCRG_ENOSYS when the request has no resident form.
+ * No counterpart in the reference. */
+int mcrg_batch_schedule(const mcrg_request* r, int32_t device, int32_t* threads, double* s_sample,
+                        double* s_tiled);
+/* Persistent batch launches and CUDA graph instantiations so far on a
+ * device.  No counterpart in the reference. */
+int mcrg_batch_stats(int32_t device, int64_t* launches, int64_t* graph_builds);
 
 /* ---------------------------------------------------------------------- */
 /* Serving: continuous batching of MCRG requests.                          */

@@ -24,7 +24,8 @@ from . import _abi
 from ._abi import MCRGError, check, lib
 from .tmatrix import MomentSums, eigenvalues, jackknife, nu
 
-__all__ = ["Lattice", "IsingModel", "MonteCarloRenormalizationGroup", "MomentSums", "batch_run", "Server",
+__all__ = ["Lattice", "IsingModel", "MonteCarloRenormalizationGroup", "MomentSums", "batch_run", "batch_schedule",
+           "batch_stats", "Server",
            "block_lattice", "lattice_couplings", "thresholds", "moments_from_c", "MCRGError", "lib",
            "nearest_neighbors", "next_nearest_neighbors"]
 
@@ -403,6 +404,23 @@ def batch_run(requests, device: int = 0, use_graph: bool = True, raw: bool = Fal
     if raw:
         return res
     return [(int(r.status), moments_from_c(r.moments) if r.status == 0 else None) for r in res]
+
+
+def batch_schedule(request: _abi.Request, device: int = 0) -> dict:
+    """The autotuned schedule of the request's chain shape (mcrg_batch_schedule):
+    threads per chain, seconds per sample in a full wave, seconds per sample on
+    the tiled HBM path (-1 when not timed)."""
+    t, s, h = C.c_int32(), C.c_double(), C.c_double()
+    check(lib().mcrg_batch_schedule(C.byref(request), device, C.byref(t), C.byref(s), C.byref(h)),
+          "mcrg_batch_schedule")
+    return {"threads": t.value, "s_per_sample": s.value, "s_per_sample_tiled": h.value}
+
+
+def batch_stats(device: int = 0) -> dict:
+    """Persistent batch launches and CUDA graph instantiations so far (mcrg_batch_stats)."""
+    a, b = C.c_int64(), C.c_int64()
+    check(lib().mcrg_batch_stats(device, C.byref(a), C.byref(b)), "mcrg_batch_stats")
+    return {"launches": a.value, "graph_builds": b.value}
 
 
 class Server:

@@ -98,6 +98,8 @@ _SIGS = {
     "mcrg_lattice_couplings": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, P(C.c_int64), C.c_int32]),
     "mcrg_lattice_couplings_noalloc": (C.c_int, [C.c_int32, C.c_void_p, C.c_int32, P(C.c_int64), C.c_int32]),
     "mcrg_batch_run": (C.c_int, [P(Request), C.c_int32, P(Result), C.c_int32, C.c_int32]),
+    "mcrg_batch_schedule": (C.c_int, [P(Request), C.c_int32, P(C.c_int32), P(C.c_double), P(C.c_double)]),
+    "mcrg_batch_stats": (C.c_int, [C.c_int32, P(C.c_int64), P(C.c_int64)]),
     "mcrg_server_create": (C.c_int, [P(C.c_void_p), P(ServerCfg)]),
     "mcrg_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_uint64)]),
     "mcrg_poll": (C.c_int, [C.c_void_p, C.c_uint64, P(Result)]),

@@ -142,34 +142,99 @@ int run_tiled_request(const mcrg_request* r, int device, mcrg_moments* out) {
   return rc;
 }
 
-// Device buffers, pinned staging and streams of mcrg_batch_run, kept per
-// device between calls so a batch does not pay allocation or stream set-up.
-constexpr int kMaxGroups = 8;
+// ---------------------------------------------------------------------------
+// Chain shapes, the schedule autotuner and packs of the persistent launch
+// ---------------------------------------------------------------------------
+// Chain form: bit 0 = levels of side >= 64 as bit planes (fast acceptance
+// regime), bit 1 = cluster updates.
+int chain_mode(const mcrg_request* r) {
+  return (make_accept(r->K).fast && r->L >= 64 ? 1 : 0) | (r->flags ? 2 : 0);
+}
 
+int pack_stride(int L, int nl, int C, int mode, int threads) {
+  return (make_plan(L, nl, C, (mode & 1) != 0, (mode & 2) != 0, threads).bytes + 15) / 16 * 16;
+}
+
+// Threads per chain the autotuner tries for a shape.  Every candidate gives
+// the same chain bit for bit (the Philox stream is keyed by site, not thread).
+std::vector<int> candidate_threads(int L, int mode) {
+  if (mode & 2) {  // cluster labelling: latency-bound, wide groups
+    if (L <= 32) return {32};
+    if (L == 64) return {128, 256, 512};
+    return {256, 512};
+  }
+  if (L <= 16) return {32};
+  if (L == 32) return {32, 64};
+  if (L == 64) return {32, 64, 128};
+  if (L == 128) return {64, 128, 256};
+  if (L == 256) return {128, 256, 512};
+  return {256, 512};
+}
+
+struct Schedule {
+  int threads = 0;       // threads per chain
+  double s_sample = 0;   // seconds per sample of one chain in a full wave of the trial
+  double s_tiled = -1;   // seconds per sample of the same chain on the HBM path (-1: not timed)
+};
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, Schedule> g_tune;  // (device, L, mode, levels, couplings)
+
+// Resident sides at which the autotuner also times the HBM path.
+bool tiled_candidate(int L, int mode) { return mode == 1 && L > MCRG_SMEM_MAX_L; }
+
+// A pool packing for chains of one shape at CTA width W.
+bool pack_geometry(int L, int nl, int C, int mode, int g, int W, int* per_pack, int* stride) {
+  if (g > W || W % g) return false;
+  *stride = pack_stride(L, nl, C, mode, g);
+  int m = std::min(W / g, kPoolMaxGroups);
+  while (m > 0 && m * *stride > kPoolMaxSmem) --m;
+  *per_pack = m;
+  return m > 0;
+}
+
+// Device buffers, pinned staging, stream and the instantiated graph of the
+// persistent batch, kept per device between calls: a batch pays neither
+// allocation nor graph instantiation unless it outgrows them.
 struct BatchWorkspace {
   std::mutex mu;
   bool ready = false;
+  int sms = 0;
+  cudaStream_t s0 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   uint8_t* d_state = nullptr;
   size_t state_cap = 0;
-  mcrg_moments* d_bins = nullptr;
+  uint8_t* d_buf = nullptr;  // [PoolQueue | packs | jobs]
+  uint8_t* h_buf = nullptr;  // pinned twin of d_buf
+  size_t buf_cap = 0;
+  uint8_t* d_out = nullptr;  // [pack counter (256 B) | bins]
   mcrg_moments* h_bins = nullptr;  // pinned
   size_t bins_cap = 0;
-  ChainJob* d_jobs = nullptr;
-  ChainJob* h_jobs = nullptr;      // pinned
-  size_t jobs_cap = 0;
-  cudaStream_t s0 = nullptr;
-  cudaStream_t ss[kMaxGroups] = {};
-  cudaEvent_t ev[kMaxGroups + 1] = {};
+  // the graph: upload, clear, persistent kernel, download
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t n_up = nullptr, n_clr = nullptr, n_run = nullptr, n_down = nullptr;
+  std::tuple<int, int, int, void*, void*> graph_key{0, 0, 0, nullptr, nullptr};
+  int64_t n_runs = 0, n_graph_builds = 0;  // persistent launches, graph instantiations
 
-  int reserve(size_t state_bytes, size_t n_bins, size_t n_jobs) {
-    if (!ready) {
-      if (cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
-      for (auto& x : ss)
-        if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
-      for (auto& e : ev)
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return MCRG_EIO;
-      ready = true;
-    }
+  int init(int device) {
+    if (ready) return MCRG_OK;
+    if (cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MCRG_EIO;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) return MCRG_EIO;
+    ready = true;
+    return MCRG_OK;
+  }
+
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    graph_key = std::make_tuple(0, 0, 0, nullptr, nullptr);
+  }
+
+  int reserve(size_t state_bytes, size_t buf_bytes, size_t n_bins) {
     if (state_bytes > state_cap) {
       cudaFree(d_state);
       d_state = nullptr;
@@ -177,35 +242,233 @@ struct BatchWorkspace {
       if (cudaMalloc(&d_state, state_bytes) != cudaSuccess) return MCRG_ENOMEM;
       state_cap = state_bytes;
     }
+    if (buf_bytes > buf_cap) {
+      drop_graph();
+      cudaFree(d_buf);
+      cudaFreeHost(h_buf);
+      d_buf = h_buf = nullptr;
+      buf_cap = 0;
+      if (cudaMalloc(&d_buf, buf_bytes) != cudaSuccess || cudaMallocHost(&h_buf, buf_bytes) != cudaSuccess)
+        return MCRG_ENOMEM;
+      buf_cap = buf_bytes;
+    }
     if (n_bins > bins_cap) {
-      cudaFree(d_bins);
+      drop_graph();
+      cudaFree(d_out);
       cudaFreeHost(h_bins);
-      d_bins = nullptr;
+      d_out = nullptr;
       h_bins = nullptr;
       bins_cap = 0;
-      if (cudaMalloc(&d_bins, sizeof(mcrg_moments) * n_bins) != cudaSuccess ||
+      if (cudaMalloc(&d_out, 256 + sizeof(mcrg_moments) * n_bins) != cudaSuccess ||
           cudaMallocHost(&h_bins, sizeof(mcrg_moments) * n_bins) != cudaSuccess)
         return MCRG_ENOMEM;
       bins_cap = n_bins;
     }
-    if (n_jobs > jobs_cap) {
-      cudaFree(d_jobs);
-      cudaFreeHost(h_jobs);
-      d_jobs = nullptr;
-      h_jobs = nullptr;
-      jobs_cap = 0;
-      if (cudaMalloc(&d_jobs, sizeof(ChainJob) * n_jobs) != cudaSuccess ||
-          cudaMallocHost(&h_jobs, sizeof(ChainJob) * n_jobs) != cudaSuccess)
-        return MCRG_ENOMEM;
-      jobs_cap = n_jobs;
-    }
     return MCRG_OK;
+  }
+
+  mcrg_moments* d_bins() { return reinterpret_cast<mcrg_moments*>(d_out + 256); }
+
+  // Issues upload, clear, persistent launch and download on s0: through the
+  // graph (built once per CTA width / grid / shared memory and buffers, its
+  // copy sizes updated per call) or directly.
+  int run(int W, int grid, int smem, size_t up_bytes, size_t n_bins, bool use_graph) {
+    const size_t clr = 256 + sizeof(mcrg_moments) * n_bins;
+    const size_t down = sizeof(mcrg_moments) * std::max<size_t>(n_bins, 1);
+    void* q = d_buf;
+    void* args[] = {&q};
+    if (!use_graph) {
+      if (cudaMemcpyAsync(d_buf, h_buf, up_bytes, cudaMemcpyHostToDevice, s0) != cudaSuccess ||
+          cudaMemsetAsync(d_out, 0, clr, s0) != cudaSuccess ||
+          cudaLaunchKernel(pool_kernel_fn(W), dim3(grid), dim3(W), args, (size_t)smem, s0) != cudaSuccess)
+        return MCRG_EIO;
+      if (n_bins && cudaMemcpyAsync(h_bins, d_bins(), down, cudaMemcpyDeviceToHost, s0) != cudaSuccess)
+        return MCRG_EIO;
+      return MCRG_OK;
+    }
+    const auto key = std::make_tuple(W, grid, smem, (void*)d_buf, (void*)d_out);
+    if (!exec || key != graph_key) {
+      drop_graph();
+      if (cudaGraphCreate(&graph, 0) != cudaSuccess) return MCRG_EIO;
+      cudaMemsetParams ms;
+      memset(&ms, 0, sizeof ms);
+      ms.dst = d_out;
+      ms.elementSize = 1;
+      ms.width = clr;
+      ms.height = 1;
+      cudaKernelNodeParams kp;
+      memset(&kp, 0, sizeof kp);
+      kp.func = const_cast<void*>(pool_kernel_fn(W));
+      kp.gridDim = dim3(grid);
+      kp.blockDim = dim3(W);
+      kp.sharedMemBytes = (unsigned)smem;
+      kp.kernelParams = args;
+      if (cudaGraphAddMemcpyNode1D(&n_up, graph, nullptr, 0, d_buf, h_buf, up_bytes, cudaMemcpyHostToDevice) !=
+              cudaSuccess ||
+          cudaGraphAddMemsetNode(&n_clr, graph, &n_up, 1, &ms) != cudaSuccess ||
+          cudaGraphAddKernelNode(&n_run, graph, &n_clr, 1, &kp) != cudaSuccess ||
+          cudaGraphAddMemcpyNode1D(&n_down, graph, &n_run, 1, h_bins, d_bins(), down, cudaMemcpyDeviceToHost) !=
+              cudaSuccess ||
+          cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+        drop_graph();
+        return MCRG_EIO;
+      }
+      graph_key = key;
+      ++n_graph_builds;
+    } else {
+      cudaMemsetParams ms;
+      memset(&ms, 0, sizeof ms);
+      ms.dst = d_out;
+      ms.elementSize = 1;
+      ms.width = clr;
+      ms.height = 1;
+      if (cudaGraphExecMemcpyNodeSetParams1D(exec, n_up, d_buf, h_buf, up_bytes, cudaMemcpyHostToDevice) !=
+              cudaSuccess ||
+          cudaGraphExecMemsetNodeSetParams(exec, n_clr, &ms) != cudaSuccess ||
+          cudaGraphExecMemcpyNodeSetParams1D(exec, n_down, h_bins, d_bins(), down, cudaMemcpyDeviceToHost) !=
+              cudaSuccess)
+        return MCRG_EIO;
+    }
+    return cudaGraphLaunch(exec, s0) == cudaSuccess ? MCRG_OK : MCRG_EIO;
   }
 };
 
 BatchWorkspace& workspace(int device) {
   static BatchWorkspace ws[64];
   return ws[device & 63];
+}
+
+// Lays out [PoolQueue | packs | jobs] in the workspace's pinned staging with
+// device pointers, and returns the bytes used.
+size_t stage_queue(BatchWorkspace& w, const std::vector<PoolPack>& packs, const std::vector<ChainJob>& jobs) {
+  const size_t off_packs = 64;
+  const size_t off_jobs = (off_packs + sizeof(PoolPack) * packs.size() + 255) & ~size_t(255);
+  PoolQueue q;
+  memset(&q, 0, sizeof q);
+  q.n_packs = (int32_t)packs.size();
+  q.packs = reinterpret_cast<const PoolPack*>(w.d_buf + off_packs);
+  q.jobs = reinterpret_cast<const ChainJob*>(w.d_buf + off_jobs);
+  q.next = reinterpret_cast<unsigned*>(w.d_out);
+  memcpy(w.h_buf, &q, sizeof q);
+  if (!packs.empty()) memcpy(w.h_buf + off_packs, packs.data(), sizeof(PoolPack) * packs.size());
+  if (!jobs.empty()) memcpy(w.h_buf + off_jobs, jobs.data(), sizeof(ChainJob) * jobs.size());
+  return off_jobs + sizeof(ChainJob) * jobs.size();
+}
+
+size_t queue_bytes(size_t n_packs, size_t n_jobs) {
+  return ((64 + sizeof(PoolPack) * n_packs + 255) & ~size_t(255)) + sizeof(ChainJob) * n_jobs;
+}
+
+// One trial of the autotuner: a full wave of chains of one shape at `g`
+// threads each, S samples per chain; returns seconds per sample of a chain
+// (the wave's time / S) or -1 when the shape does not fit that way.
+double trial_pool(BatchWorkspace& w, int L, int nl, int C, int mode, int g) {
+  const int W = g > 256 ? 512 : 256;
+  int m = 0, stride = 0, occ = 0;
+  if (!pack_geometry(L, nl, C, mode, g, W, &m, &stride)) return -1;
+  if (pool_prepare(W, m * stride, &occ) != cudaSuccess || occ < 1) return -1;
+  const int n_chains = std::min(w.sms * occ * m, 4096);
+  const int S = std::max(2, std::min(64, 262144 / (L * L)));
+  std::vector<ChainJob> jobs((size_t)n_chains);
+  std::vector<PoolPack> packs;
+  if (w.reserve((size_t)n_chains * L * L + 16, queue_bytes((size_t)n_chains, (size_t)n_chains), (size_t)n_chains))
+    return -1;
+  mcrg_request r;
+  memset(&r, 0, sizeof r);
+  r.L = L;
+  r.n_couplings = C;
+  r.K = -0.44068679350977147;  // critical coupling: the open-site rate of the batched workloads
+  r.flags = (mode & 2) ? MCRG_UPDATE_SWENDSEN_WANG : 0;
+  r.n_samples = S;
+  r.sweeps_between = 1;
+  for (int i = 0; i < n_chains; ++i) {
+    r.seed = 0x7A11u + (uint64_t)i;
+    fill_job(&jobs[(size_t)i], &r, nl, w.d_state + (size_t)i * L * L, w.d_bins() + i);
+    jobs[(size_t)i].threads = g;
+    jobs[(size_t)i].store = 0;
+  }
+  for (int i = 0; i < n_chains; i += m) packs.push_back(PoolPack{i, (int16_t)std::min(m, n_chains - i), (int16_t)g, stride, 0});
+  const size_t up = stage_queue(w, packs, jobs);
+  const int grid = std::min((int)packs.size(), w.sms * occ);
+  double best = -1;
+  for (int rep = 0; rep < 3; ++rep) {
+    if (cudaEventRecord(w.e0, w.s0) != cudaSuccess || w.run(W, grid, m * stride, up, 0, false) != MCRG_OK ||
+        cudaEventRecord(w.e1, w.s0) != cudaSuccess || cudaEventSynchronize(w.e1) != cudaSuccess)
+      return -1;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, w.e0, w.e1);
+    if (rep > 0 && (best < 0 || ms < best)) best = ms;  // first run: warm-up
+  }
+  return best * 1e-3 / S;
+}
+
+double trial_tiled(int device, int L, int nl, int C) {
+  mcrg_cfg cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.L = L;
+  cfg.b = 2;
+  cfg.n_levels = nl;
+  cfg.n_couplings = C;
+  cfg.K = -0.44068679350977147;
+  cfg.seed = 0x7A11u;
+  cfg.device = device;
+  mcrg_ctx* c = nullptr;
+  if (mcrg_alloc(&c, &cfg)) return -1;
+  mcrg_moments m;
+  const int S = 8;
+  double best = -1;
+  for (int rep = 0; rep < 3 && c; ++rep) {
+    const double t0 = mono_s();
+    if (mcrg_measure(c, S, 1, &m, 0, nullptr, 0)) break;
+    const double dt = mono_s() - t0;
+    if (rep > 0 && (best < 0 || dt < best)) best = dt;
+  }
+  mcrg_free(c);
+  return best > 0 ? best / S : -1;
+}
+
+// The schedule of a shape: cached, or tuned now by timed trials on the
+// workspace's stream.  MCRG_POOL_THREADS=<threads> forces the threads per
+// chain of every shape it is a candidate for (not cached).
+Schedule schedule_for(BatchWorkspace& w, int device, int L, int nl, int C, int mode) {
+  const char* force = getenv("MCRG_POOL_THREADS");
+  int forced = force ? atoi(force) : 0;
+  {
+    const std::vector<int> cand = candidate_threads(L, mode);
+    if (std::find(cand.begin(), cand.end(), forced) == cand.end()) forced = 0;
+  }
+  const auto key = std::make_tuple(device, L, mode, nl, C);
+  if (!forced) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second;
+  }
+  Schedule best;
+  double best_rate = -1;
+  for (int g : candidate_threads(L, mode)) {
+    if (forced && g != forced) continue;
+    const double t = trial_pool(w, L, nl, C, mode, g);
+    if (t <= 0) continue;
+    int m = 0, stride = 0, occ = 0;
+    const int W = g > 256 ? 512 : 256;
+    pack_geometry(L, nl, C, mode, g, W, &m, &stride);
+    pool_prepare(W, m * stride, &occ);
+    const double rate = (double)w.sms * occ * m / t;  // chain samples per second over the device
+    if (rate > best_rate) {
+      best_rate = rate;
+      best.threads = g;
+      best.s_sample = t;
+    }
+  }
+  if (!best.threads) {  // nothing fit (should not happen for resident shapes): the fixed rule
+    best.threads = resident_threads(L, (mode & 2) != 0);
+    best.s_sample = 0;
+  }
+  if (forced) return best;
+  if (tiled_candidate(L, mode)) best.s_tiled = trial_tiled(device, L, nl, C);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  return best;
 }
 
 }  // namespace
@@ -222,100 +485,159 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     nl[i] = check_request(&reqs[i]);
     results[i].status = nl[i] < 0 ? nl[i] : MCRG_OK;
   }
-  // group resident requests by side and chain form (bit planes, cluster updates)
-  std::map<std::pair<int, int>, std::vector<int>> groups;
+  // resident requests by shape (side, chain form)
+  std::map<std::pair<int, int>, std::vector<int>> shapes;
   std::vector<int> tiled;
-  size_t state_bytes = 0;
-  int64_t total_bins = 0;
-  std::vector<size_t> state_off(n, 0);
-  std::vector<int64_t> bin_off(n, 0);
   for (int i = 0; i < n; ++i) {
     if (results[i].status) continue;
-    if (runs_resident(&reqs[i], nl[i])) {
-      const int mode = (make_accept(reqs[i].K).fast && reqs[i].L >= 64 ? 1 : 0) | (reqs[i].flags ? 2 : 0);
-      groups[{reqs[i].L, mode}].push_back(i);
-      state_off[i] = state_bytes;
-      state_bytes += (size_t)reqs[i].L * reqs[i].L;
-      bin_off[i] = total_bins;
-      total_bins += n_dev_bins(&reqs[i]);
-    } else {
-      tiled.push_back(i);
-    }
+    if (runs_resident(&reqs[i], nl[i])) shapes[{reqs[i].L, chain_mode(&reqs[i])}].push_back(i);
+    else tiled.push_back(i);
   }
   int rc = MCRG_OK;
-  if (!groups.empty()) {
+  if (!shapes.empty()) {
     BatchWorkspace& w = workspace(device);
     std::lock_guard<std::mutex> lk(w.mu);
-    std::vector<std::pair<int, int>> ranges;  // (first job, count) per group
-    std::vector<int> modes;                   // chain form per group
-    std::vector<int> order;                   // job index -> request index
-    const size_t n_jobs = (size_t)n - tiled.size() - (size_t)std::count_if(results, results + n, [](const mcrg_result& r) {
-                            return r.status != MCRG_OK;
-                          });
-    const size_t nb = (size_t)(total_bins > 0 ? total_bins : 1);
-    rc = w.reserve(state_bytes + 16, nb, n_jobs);
-    if (!rc) {
-      // largest sides first so the longest chains start earliest
-      size_t k = 0;
-      for (auto it = groups.rbegin(); it != groups.rend(); ++it) {
-        ranges.push_back({(int)k, (int)it->second.size()});
-        modes.push_back(it->first.second);
-        for (int i : it->second) {
-          fill_job(&w.h_jobs[k++], &reqs[i], nl[i], w.d_state + state_off[i], w.d_bins + bin_off[i]);
-          order.push_back(i);
-        }
+    rc = w.init(device);
+    // schedules (autotuned once per shape), the CTA width and the packs
+    struct Shape {
+      int L, mode, nl, C, g, per_pack, stride;
+      std::vector<int> reqs;
+    };
+    std::vector<Shape> sh;
+    int W = 256;
+    const char* se = getenv("MCRG_BATCH_SCHEDULE");
+    const int sched_env = !se ? 0 : (!strcmp(se, "resident") ? 1 : (!strcmp(se, "tiled") ? 2 : 0));
+    for (auto& kv : shapes) {
+      if (rc) break;
+      Shape s{kv.first.first, kv.first.second, 0, 0, 0, 0, 0, kv.second};
+      for (int i : s.reqs) {
+        s.nl = std::max(s.nl, nl[i]);
+        s.C = std::max(s.C, reqs[i].n_couplings);
       }
-      cudaStream_t s0 = w.s0;
-      cudaMemcpyAsync(w.d_jobs, w.h_jobs, sizeof(ChainJob) * n_jobs, cudaMemcpyHostToDevice, s0);
-      cudaMemsetAsync(w.d_bins, 0, sizeof(mcrg_moments) * nb, s0);
-      cudaGraph_t graph = nullptr;
-      cudaGraphExec_t exec = nullptr;
-      if (use_graph) cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal);
-      cudaEventRecord(w.ev[kMaxGroups], s0);
-      for (size_t g = 0; g < ranges.size(); ++g) {
-        cudaStream_t sg = w.ss[g % kMaxGroups];
-        cudaStreamWaitEvent(sg, w.ev[kMaxGroups], 0);
-        const ChainJob& j0 = w.h_jobs[(size_t)ranges[g].first];
-        int maxlev = 0;
-        for (int q = 0; q < ranges[g].second; ++q) maxlev = std::max(maxlev, w.h_jobs[(size_t)ranges[g].first + q].n_levels);
-        if (launch_chain(w.d_jobs + ranges[g].first, ranges[g].second, j0.L, maxlev, MCRG_MAX_COUPLINGS, j0.threads,
-                         (modes[g] & 1) != 0, sg, (modes[g] & 2) != 0) != cudaSuccess)
-          rc = MCRG_EIO;
-        cudaEventRecord(w.ev[g % kMaxGroups], sg);
-        cudaStreamWaitEvent(s0, w.ev[g % kMaxGroups], 0);
+      const Schedule sc = schedule_for(w, device, s.L, s.nl, s.C, s.mode);
+      // resident vs tiled for the largest sides: tiled when running them one after
+      // another on the whole device ends before a single resident chain would
+      // (MCRG_BATCH_SCHEDULE=resident / tiled forces one)
+      const bool go_tiled =
+          tiled_candidate(s.L, s.mode) &&
+          (sched_env == 2 ||
+           (sched_env == 0 && sc.s_tiled > 0 && sc.s_sample > 0 && (double)s.reqs.size() * sc.s_tiled < sc.s_sample));
+      if (go_tiled) {
+        tiled.insert(tiled.end(), s.reqs.begin(), s.reqs.end());
+        continue;
       }
-      if (use_graph) {
-        if (cudaStreamEndCapture(s0, &graph) != cudaSuccess ||
-            cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess || cudaGraphLaunch(exec, s0) != cudaSuccess)
-          rc = MCRG_EIO;
+      s.g = sc.threads;
+      W = std::max(W, s.g > 256 ? 512 : 256);
+      sh.push_back(s);
+    }
+    std::vector<PoolPack> packs;
+    std::vector<ChainJob> jobs;
+    std::vector<int> order;  // job index -> request
+    std::vector<size_t> state_off(n, 0);
+    std::vector<int64_t> bin_off(n, 0);
+    size_t state_bytes = 0;
+    int64_t total_bins = 0;
+    int smem = 16;
+    std::vector<std::pair<double, PoolPack>> costed;
+    for (auto& s : sh) {
+      if (rc) break;
+      if (!pack_geometry(s.L, s.nl, s.C, s.mode, s.g, W, &s.per_pack, &s.stride)) {
+        rc = MCRG_EINVAL;
+        break;
       }
-      if (total_bins > 0)
-        cudaMemcpyAsync(w.h_bins, w.d_bins, sizeof(mcrg_moments) * (size_t)total_bins, cudaMemcpyDeviceToHost, s0);
-      if (cudaStreamSynchronize(s0) != cudaSuccess) rc = MCRG_EIO;
-      const double t_done = mono_s();
-      for (int i : order) {
-        const int64_t nbi = n_dev_bins(&reqs[i]);
-        if (nbi == 1) {
-          results[i].moments = w.h_bins[(size_t)bin_off[i]];
-        } else {
+      auto cost = [&](int i) {
+        const mcrg_request& q = reqs[i];
+        return (double)q.L * q.L * (double)(q.n_eq + q.n_samples * (q.sweeps_between + 1));
+      };
+      std::stable_sort(s.reqs.begin(), s.reqs.end(), [&](int a, int b) { return cost(a) > cost(b); });
+      for (size_t k = 0; k < s.reqs.size(); k += (size_t)s.per_pack) {
+        const int cnt = (int)std::min(s.reqs.size() - k, (size_t)s.per_pack);
+        costed.push_back({cost(s.reqs[k]), PoolPack{(int32_t)(jobs.size() + k), (int16_t)cnt, (int16_t)s.g, s.stride, 0}});
+      }
+      for (int i : s.reqs) {
+        state_off[i] = state_bytes;
+        state_bytes += (size_t)reqs[i].L * reqs[i].L;
+        bin_off[i] = total_bins;
+        total_bins += n_dev_bins(&reqs[i]);
+        jobs.emplace_back();
+        order.push_back(i);
+      }
+      smem = std::max(smem, s.per_pack * s.stride);
+    }
+    // longest packs first: the tail of the launch is short chains
+    std::stable_sort(costed.begin(), costed.end(),
+                     [](const std::pair<double, PoolPack>& a, const std::pair<double, PoolPack>& b) {
+                       return a.first > b.first;
+                     });
+    for (auto& c : costed) packs.push_back(c.second);
+    if (!rc && !jobs.empty()) {
+      rc = w.reserve(state_bytes + 16, queue_bytes(packs.size(), jobs.size()), (size_t)std::max<int64_t>(total_bins, 1));
+      if (!rc) {
+        size_t k = 0;
+        for (auto& s : sh)
+          for (int i : s.reqs) {
+            fill_job(&jobs[k], &reqs[i], nl[i], w.d_state + state_off[i], w.d_bins() + bin_off[i]);
+            jobs[k].threads = s.g;
+            ++k;
+          }
+        int occ = 0;
+        if (pool_prepare(W, smem, &occ) != cudaSuccess || occ < 1) rc = MCRG_EIO;
+        const int grid = std::min((int)packs.size(), w.sms * std::max(occ, 1));
+        const size_t up = stage_queue(w, packs, jobs);
+        if (!rc) rc = w.run(W, grid, smem, up, (size_t)total_bins, use_graph != 0);
+        ++w.n_runs;
+        if (cudaStreamSynchronize(w.s0) != cudaSuccess) rc = MCRG_EIO;
+        const double t_done = mono_s();
+        for (int i : order) {
+          const int64_t nbi = n_dev_bins(&reqs[i]);
+          if (nbi == 1) {
+            results[i].moments = w.h_bins[(size_t)bin_off[i]];
+          } else {
+            for (int64_t q = 0; q < nbi; ++q) add_into(&results[i].moments, &w.h_bins[(size_t)(bin_off[i] + q)]);
+          }
           results[i].moments.n_levels = nl[i];
           results[i].moments.n_couplings = reqs[i].n_couplings;
-          for (int64_t q = 0; q < nbi; ++q) add_into(&results[i].moments, &w.h_bins[(size_t)(bin_off[i] + q)]);
+          results[i].done_s = t_done;
+          if (rc) results[i].status = rc;
         }
-        results[i].moments.n_levels = nl[i];
-        results[i].moments.n_couplings = reqs[i].n_couplings;
-        results[i].done_s = t_done;
-        if (rc) results[i].status = rc;
       }
-      if (exec) cudaGraphExecDestroy(exec);
-      if (graph) cudaGraphDestroy(graph);
     }
+    if (rc)
+      for (auto& s : sh)
+        for (int i : s.reqs) results[i].status = rc;
   }
   for (int i : tiled) {
     results[i].status = run_tiled_request(&reqs[i], device, &results[i].moments);
     results[i].done_s = mono_s();
   }
   return rc;
+}
+
+extern "C" int mcrg_batch_schedule(const mcrg_request* r, int32_t device, int32_t* threads, double* s_sample,
+                                   double* s_tiled) {
+  if (!r || !threads) return MCRG_EINVAL;
+  const int nl = check_request(r);
+  if (nl < 0) return nl;
+  if (!runs_resident(r, nl)) return MCRG_ENOSYS;
+  if (cudaSetDevice(device) != cudaSuccess) return MCRG_EIO;
+  BatchWorkspace& w = workspace(device);
+  std::lock_guard<std::mutex> lk(w.mu);
+  const int rc = w.init(device);
+  if (rc) return rc;
+  const Schedule sc = schedule_for(w, device, r->L, nl, r->n_couplings, chain_mode(r));
+  *threads = sc.threads;
+  if (s_sample) *s_sample = sc.s_sample;
+  if (s_tiled) *s_tiled = sc.s_tiled;
+  return MCRG_OK;
+}
+
+extern "C" int mcrg_batch_stats(int32_t device, int64_t* launches, int64_t* graph_builds) {
+  if (device < 0 || device >= 64) return MCRG_EINVAL;
+  BatchWorkspace& w = workspace(device);
+  std::lock_guard<std::mutex> lk(w.mu);
+  if (launches) *launches = w.n_runs;
+  if (graph_builds) *graph_builds = w.n_graph_builds;
+  return MCRG_OK;
 }
 
 // ===========================================================================

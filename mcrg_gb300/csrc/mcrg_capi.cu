@@ -39,6 +39,7 @@ struct mcrg_ctx {
   unsigned long long* d_cl = nullptr;  // cluster updates: [0] flipped spins, [1] error flags
   mcrg_moments* d_cbins = nullptr;     // cluster measurement: one bin per sample of a chunk
   ChainJob* d_cjobs = nullptr;         // cluster measurement: one measurement job per sample of a chunk
+  DevSpan* span = nullptr;             // where device buffers come from (nullptr: cudaMalloc)
 };
 
 namespace {
@@ -180,10 +181,10 @@ void add_moments(mcrg_moments* dst, const mcrg_moments* src) {
 
 int ensure_bins(mcrg_ctx* c, int64_t n) {
   if (n <= c->bins_cap) return MCRG_OK;
-  if (c->d_bins) cudaFree(c->d_bins);
+  dev_release(c->span, c->d_bins);
   c->d_bins = nullptr;
   c->bins_cap = 0;
-  if (cudaMalloc(&c->d_bins, sizeof(mcrg_moments) * (size_t)n) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(c->span, &c->d_bins, sizeof(mcrg_moments) * (size_t)n) != cudaSuccess) return MCRG_ENOMEM;
   c->bins_cap = n;
   return MCRG_OK;
 }
@@ -304,7 +305,63 @@ int mcrg_thresholds(double K, uint32_t thr[5], uint8_t always[5]) {
   return MCRG_OK;
 }
 
-int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
+int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) { return context_create(out, cfg, nullptr); }
+
+}  // extern "C"
+
+namespace mcrg {
+
+cudaError_t dev_alloc(DevSpan* s, void** p, size_t bytes) {
+  if (!s) return cudaMalloc(p, bytes);
+  if (bytes == 0) bytes = 1;
+  const size_t off = (s->used + 255) & ~size_t(255);
+  if (off > s->cap || bytes > s->cap - off) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  s->live.push_back({off, bytes});
+  s->used = off + bytes;
+  *p = s->base + off;
+  return cudaSuccess;
+}
+
+void dev_release(DevSpan* s, void* p) {
+  if (!p) return;
+  if (!s) {
+    cudaFree(p);
+    return;
+  }
+  const size_t off = (size_t)(static_cast<uint8_t*>(p) - s->base);
+  for (auto& e : s->live)
+    if (e.first == off && e.second) {
+      e.second = 0;
+      break;
+    }
+  while (!s->live.empty() && s->live.back().second == 0) s->live.pop_back();
+  s->used = s->live.empty() ? 0 : s->live.back().first + s->live.back().second;
+}
+
+size_t context_bytes(int L, int n_levels, int C, int update, int64_t n_samples) {
+  auto a = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t LL = (size_t)L * L;
+  const int64_t nb = n_samples > 0 ? (n_samples + kMaxDeviceBin - 1) / kMaxDeviceBin : 1;
+  size_t b = a(sizeof(ChainJob)) + a(LL) + a(sizeof(int) * 64);  // job, natural staging, flags
+  if (L <= MCRG_SMEM_MAX_L) {
+    b += a(LL);  // state
+  } else {       // ping-pong buffers, blocked levels (< LL / 3), sums, status, bins of the tiled path
+    b += 2 * a(LL) + a(LL / 3 + 16) + a(sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) +
+         a(sizeof(int)) + a(sizeof(mcrg_moments) * (size_t)nb);
+  }
+  b += a(sizeof(mcrg_moments) * (size_t)nb);  // the context's bins
+  if (update)  // labels, counters, one chunk of per-sample bins and measurement jobs
+    b += a(sizeof(int) * LL) + a(2 * sizeof(unsigned long long)) + a(sizeof(mcrg_moments) * 256) +
+         a(sizeof(ChainJob) * 256);
+  (void)n_levels;
+  (void)C;
+  return b + 4096;
+}
+
+int context_create(mcrg_ctx** out, const mcrg_cfg* cfg, DevSpan* span) {
   if (!out || !cfg) return MCRG_EINVAL;
   *out = nullptr;
   if (!valid_L(cfg->L) || cfg->b != 2 || cfg->n_couplings < 1 || cfg->n_couplings > MCRG_MAX_COUPLINGS ||
@@ -320,16 +377,18 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
   c->cfg = *cfg;
   c->n_levels = nl;
   c->acc = make_accept(cfg->K);
+  c->span = span;
+  c->tiled.span = span;
   int rc = MCRG_OK;
   const size_t LL = (size_t)cfg->L * cfg->L;
   do {
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = MCRG_EIO; break; }
-    if (cudaMalloc(&c->d_job, sizeof(ChainJob)) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
-    if (cudaMalloc(&c->d_nat, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
-    if (cudaMalloc(&c->d_flag, sizeof(int) * 64) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    if (dev_alloc(span, &c->d_job, sizeof(ChainJob)) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    if (dev_alloc(span, &c->d_nat, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    if (dev_alloc(span, &c->d_flag, sizeof(int) * 64) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
     const Key key{(uint32_t)cfg->seed, (uint32_t)(cfg->seed >> 32)};
     if (cfg->L <= MCRG_SMEM_MAX_L) {
-      if (cudaMalloc(&c->d_state, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+      if (dev_alloc(span, &c->d_state, LL) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
       ChainJob j;
       memset(&j, 0, sizeof j);
       j.L = cfg->L; j.n_levels = nl; j.C = cfg->n_couplings; j.threads = threads_for(cfg->L);
@@ -355,21 +414,26 @@ int mcrg_alloc(mcrg_ctx** out, const mcrg_cfg* cfg) {
   return MCRG_OK;
 }
 
+}  // namespace mcrg
+
+extern "C" {
+
 int mcrg_free(mcrg_ctx* c) {
   if (!c) return MCRG_EINVAL;
   cudaSetDevice(c->cfg.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->is_tiled) tiled_free(&c->tiled);
-  cudaFree(c->d_state);
-  cudaFree(c->d_job);
-  cudaFree(c->d_bins);
-  cudaFree(c->d_nat);
-  cudaFree(c->d_flag);
-  cudaFree(c->d_rgnn);
-  cudaFree(c->d_labels);
-  cudaFree(c->d_cl);
-  cudaFree(c->d_cbins);
-  cudaFree(c->d_cjobs);
+  DevSpan* sp = c->span;
+  dev_release(sp, c->d_cjobs);
+  dev_release(sp, c->d_cbins);
+  dev_release(sp, c->d_cl);
+  dev_release(sp, c->d_labels);
+  dev_release(sp, c->d_rgnn);
+  dev_release(sp, c->d_bins);
+  dev_release(sp, c->d_state);
+  dev_release(sp, c->d_flag);
+  dev_release(sp, c->d_nat);
+  dev_release(sp, c->d_job);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return MCRG_OK;
@@ -513,9 +577,9 @@ int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_mo
 static int cluster_updates(mcrg_ctx* c, int64_t n, int32_t kind) {
   const int L = c->cfg.L;
   if (!c->d_labels) {
-    if (cudaMalloc(&c->d_labels, sizeof(int) * (size_t)L * L) != cudaSuccess) return MCRG_ENOMEM;
-    if (cudaMalloc(&c->d_cl, 2 * sizeof(unsigned long long)) != cudaSuccess) {
-      cudaFree(c->d_labels);
+    if (dev_alloc(c->span, &c->d_labels, sizeof(int) * (size_t)L * L) != cudaSuccess) return MCRG_ENOMEM;
+    if (dev_alloc(c->span, &c->d_cl, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+      dev_release(c->span, c->d_labels);
       c->d_labels = nullptr;
       return MCRG_ENOMEM;
     }
@@ -584,8 +648,9 @@ int mcrg_measure_cluster(mcrg_ctx* c, int64_t n_samples, int64_t updates_between
   // chunks of samples: per sample the cluster updates and one measurement into its own device bin,
   // queued without a host round trip; one read-back per chunk
   constexpr int64_t kChunk = 256;
-  if (!c->d_cbins && cudaMalloc(&c->d_cbins, sizeof(mcrg_moments) * kChunk) != cudaSuccess) return MCRG_ENOMEM;
-  if (!c->is_tiled && !c->d_cjobs && cudaMalloc(&c->d_cjobs, sizeof(ChainJob) * kChunk) != cudaSuccess)
+  if (!c->d_cbins && dev_alloc(c->span, &c->d_cbins, sizeof(mcrg_moments) * kChunk) != cudaSuccess)
+    return MCRG_ENOMEM;
+  if (!c->is_tiled && !c->d_cjobs && dev_alloc(c->span, &c->d_cjobs, sizeof(ChainJob) * kChunk) != cudaSuccess)
     return MCRG_ENOMEM;
   std::vector<mcrg_moments> h((size_t)kChunk);
   std::vector<ChainJob> jobs(c->is_tiled ? 0 : (size_t)kChunk);
@@ -659,7 +724,7 @@ int mcrg_block(mcrg_ctx* c, int level, int8_t* host_out) {
   const uint8_t* src = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
   uint8_t* tmp = nullptr;
   const size_t LL = (size_t)L * L;
-  if (cudaMalloc(&tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(c->span, &tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
   uint8_t* buf[2] = {tmp, tmp + LL / 2};
   const uint8_t* cur = src;
   int n = L;
@@ -680,7 +745,7 @@ int mcrg_block(mcrg_ctx* c, int level, int8_t* host_out) {
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
   if (!rc) rc = sweep_status(c);
-  cudaFree(tmp);
+  dev_release(c->span, tmp);
   return rc;
 }
 
@@ -695,9 +760,9 @@ int mcrg_interactions(mcrg_ctx* c, int64_t* out) {
   uint8_t* tmp = nullptr;
   int* dS = nullptr;
   const size_t LL = (size_t)L * L;
-  if (cudaMalloc(&tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
-  if (cudaMalloc(&dS, sizeof(int) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) != cudaSuccess) {
-    cudaFree(tmp);
+  if (dev_alloc(c->span, &tmp, LL) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(c->span, &dS, sizeof(int) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) != cudaSuccess) {
+    dev_release(c->span, tmp);
     return MCRG_ENOMEM;
   }
   int rc = MCRG_OK;
@@ -720,8 +785,8 @@ int mcrg_interactions(mcrg_ctx* c, int64_t* out) {
   if (!rc && cudaMemcpyAsync(hS, dS, sizeof hS, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) rc = MCRG_EIO;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) rc = MCRG_EIO;
   if (!rc) rc = sweep_status(c);
-  cudaFree(tmp);
-  cudaFree(dS);
+  dev_release(c->span, dS);
+  dev_release(c->span, tmp);
   if (rc) return rc;
   for (int l = 0; l <= nl; ++l)
     for (int cc = 0; cc < C; ++cc) out[l * C + cc] = hS[l * MCRG_MAX_COUPLINGS + cc];
@@ -864,7 +929,7 @@ int mcrg_rgnn_scalar_output(mcrg_ctx* c, const double* W, double* out) {
   CK(cudaSetDevice(c->cfg.device));
   const int L = c->cfg.L;
   const size_t nwork = (size_t)(L / 32) * (L / 32) + (size_t)(L / 1024) * (L / 1024) + 3;
-  if (!c->d_rgnn && cudaMalloc(&c->d_rgnn, sizeof(double) * nwork) != cudaSuccess) return MCRG_ENOMEM;
+  if (!c->d_rgnn && dev_alloc(c->span, &c->d_rgnn, sizeof(double) * nwork) != cudaSuccess) return MCRG_ENOMEM;
   const uint8_t* state = c->is_tiled ? tiled_state(&c->tiled) : c->d_state;
   double* d_out = c->d_rgnn + nwork - 1;
   CK(launch_rgnn_scalar(state, L, W, c->d_rgnn, d_out, c->stream));

@@ -42,35 +42,31 @@ __device__ __forceinline__ void chain_sweep(uint8_t* lat, int L, uint32_t t, Key
     } else {
       sweep_colour_scalar(lat, L, c, t, key, rep, acc, tid, T);
     }
-    __syncthreads();
+    chain_sync(T);
   }
 }
 
 // ---------------------------------------------------------------------------
-// One chain per CTA.
+// One chain, run by T threads (tid = 0 .. T-1) on the shared memory at `smem`
+// (make_plan(L, n_levels, C, planes, cluster, T).bytes of it): the whole CTA
+// (chain_kernel) or one warp-aligned group of a CTA (pool_kernel).
 // ---------------------------------------------------------------------------
-// MAXT / MINB: launch bounds of the instantiation (256 x 3 for L <= 256, 512 x 2
-// for the plane chains of L >= 512, which run one or two CTAs per SM).
-template <int MAXT, int MINB>
-__global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __restrict__ jobs) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  const ChainJob& J = jobs[blockIdx.x];
+__device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int tid, int T) {
   const int L = J.L, nl = J.n_levels, C = J.C;
-  const int tid = threadIdx.x, T = blockDim.x;
   const Key key = J.key;
   const uint32_t rep = J.replica;
   const Accept acc = J.acc;
   // L >= 64 in the fast regime: levels of side >= 64 are plane words
   const bool bits = acc.fast && L >= 64;
   const int upd = J.update;  // 0: sweeps, else the cluster update kind
-  const SmemPlan plan = make_plan(L, nl, C, bits, upd != 0);
+  const SmemPlan plan = make_plan(L, nl, C, bits, upd != 0, T);
   uint8_t* lat = smem;
   int* S = reinterpret_cast<int*>(smem + plan.s_off);
   int2* tab = reinterpret_cast<int2*>(smem + plan.tab_off);
   long long* macc = reinterpret_cast<long long*>(smem + plan.acc_off);
   // moment entries: T-matrix moments (S, Sb S, Sb Sb) or flow moments (S_l, S_l S_0 of coupling 0)
   const int E = J.flow ? 2 * (nl + 1) : plan.E;
-  uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (threadIdx.x >> 5) * kOpenPerWarp;
+  uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + plan.scr_off) + (tid >> 5) * kOpenPerWarp;
   const bool vec = acc.fast && L >= 16;
   uint32_t* pl = bits ? reinterpret_cast<uint32_t*>(smem) : nullptr;
   int* qn = bits ? reinterpret_cast<int*>(smem + plan.qn_off) : nullptr;
@@ -113,7 +109,7 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
     macc[e] = 0;
   }
   if (bits && tid < 2) qn[tid] = 0;
-  __syncthreads();
+  chain_sync(T);
 
   // one Monte Carlo step at update index tt: a sweep, or a cluster update
   auto step = [&](uint32_t tt) {
@@ -134,7 +130,7 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
     // ---- measurement: coupling sums of every level, blocking level by level
     const uint32_t sample = J.n0 + (uint32_t)n;
     for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
-    __syncthreads();
+    chain_sync(T);
     int m = L;
     for (int l = 0; l <= nl; ++l, m >>= 1) {
       const uint8_t* lev = smem + plan.off[l];
@@ -160,7 +156,7 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
         else if (m >= 32) block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
         else block_scalar(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
       }
-      __syncthreads();
+      chain_sync(T);
     }
     // ---- moment products (each entry owned by one thread)
     for (int e = tid; e < E; e += T) {
@@ -193,7 +189,7 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
         out->n_samples = last ? (n % J.bin_size) + 1 : J.bin_size;
       }
     }
-    __syncthreads();
+    chain_sync(T);
   }
 
   // ---- final configuration back to HBM
@@ -203,6 +199,113 @@ __global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __res
     const uint4* src = reinterpret_cast<const uint4*>(lat);
     uint4* dst = reinterpret_cast<uint4*>(J.state);
     for (int v = tid; v < L * L / 16; v += T) dst[v] = src[v];
+  }
+}
+
+// One chain per CTA.  MAXT / MINB: launch bounds of the instantiation (256 x 3
+// for L <= 256, 512 x 2 for the plane chains of L >= 512, which run one or
+// two CTAs per SM).
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) chain_kernel(const ChainJob* __restrict__ jobs) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  run_chain(jobs[blockIdx.x], smem, threadIdx.x, blockDim.x);
+}
+
+// Persistent batch: every CTA takes packs from the queue in order (one
+// atomicAdd per pack) until none is left.  A pack is `count` chains of
+// `threads` threads each, laid out as consecutive warp-aligned groups of the
+// CTA with `stride` bytes of shared memory apiece; threads beyond the pack's
+// groups wait at the CTA barrier that ends the pack.  Each group copies its
+// job into shared memory first, so the chain reads its descriptor from there.
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) pool_kernel(const PoolQueue* __restrict__ q) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ int s_pack;
+  __shared__ ChainJob s_job[kPoolMaxGroups];
+  const int n_packs = q->n_packs;
+  for (;;) {
+    if (threadIdx.x == 0) s_pack = (int)atomicAdd(q->next, 1u);
+    __syncthreads();
+    const int p = s_pack;
+    if (p >= n_packs) break;
+    const PoolPack pk = q->packs[p];
+    const int g = (int)threadIdx.x / pk.threads, tid = (int)threadIdx.x - g * pk.threads;
+    if (g < pk.count) {
+      if (tid == 0) s_job[g] = q->jobs[pk.first + g];
+      chain_sync(pk.threads);
+      run_chain(s_job[g], smem + (size_t)g * pk.stride, tid, pk.threads);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The served request loop: persistent CTAs drain the host ring (ServeEntry,
+// mcrg_internal.cuh).  Every wait is bounded: a CTA with nothing to claim
+// leaves after ctl->idle_ns of device time, and the server launches the loop
+// again when entries are published while no CTA is left.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_volatile_s32(const int32_t* p) { return *reinterpret_cast<const volatile int32_t*>(p); }
+__device__ __forceinline__ void st_release_sys(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long serve_clock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__global__ void __launch_bounds__(kServeThreads, 1) serve_kernel(ServeArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  __shared__ long long s_idx;
+  __shared__ __align__(16) ServeEntry s_entry;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long got = -1;
+      const unsigned long long idle = *reinterpret_cast<const volatile unsigned long long*>(&a.ctl->idle_ns);
+      const unsigned long long t0 = serve_clock_ns();
+      unsigned ns = 128;
+      for (;;) {
+        if (ld_volatile_s32(&a.ctl->stop)) break;
+        if ((int)blockIdx.x >= (int)gridDim.x - ld_volatile_s32(&a.ctl->shrink)) break;
+        const unsigned long long tail = ld_acquire_sys(&a.ctl->tail);
+        const unsigned long long h = *reinterpret_cast<volatile unsigned long long*>(a.head);
+        if (h < tail) {
+          if (atomicCAS(a.head, h, h + 1) == h) {
+            got = (long long)h;
+            break;
+          }
+          continue;
+        }
+        if (serve_clock_ns() - t0 > idle) break;
+        __nanosleep(ns);
+        if (ns < 4096) ns <<= 1;
+      }
+      s_idx = got;
+    }
+    __syncthreads();
+    const long long idx = s_idx;
+    if (idx < 0) break;
+    // the entry into shared memory (ordered after thread 0's acquire by the barrier)
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(a.ring + (size_t)(idx % a.cap));
+      uint4* dst = reinterpret_cast<uint4*>(&s_entry);
+      for (int v = threadIdx.x; v < (int)(sizeof(ServeEntry) / 16); v += blockDim.x) dst[v] = src[v];
+    }
+    __syncthreads();
+    const PoolPack pk = s_entry.pk;
+    const int g = (int)threadIdx.x / pk.threads, tid = (int)threadIdx.x - g * pk.threads;
+    if (g < pk.count) run_chain(s_entry.jobs[g], smem + (size_t)g * pk.stride, tid, pk.threads);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence_system();
+      st_release_sys(a.done + (size_t)(idx % a.cap), (unsigned int)(idx + 1));
+    }
   }
 }
 
@@ -229,7 +332,7 @@ __global__ void couplings_once_kernel(const uint8_t* in, int N, int C, int* out)
 cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
                          cudaStream_t stream, bool cluster) {
   if (cluster && L > kClusterMaxL) return cudaErrorInvalidValue;
-  const SmemPlan plan = make_plan(L, n_levels, C, planes, cluster);
+  const SmemPlan plan = make_plan(L, n_levels, C, planes, cluster, threads);
   constexpr int kMaxSmem = 227 * 1024;  // opt-in shared memory per CTA
   if (plan.bytes > kMaxSmem || threads > 512) return cudaErrorInvalidValue;
   const bool wide = threads > 256;
@@ -249,6 +352,44 @@ cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels
   if (wide) chain_kernel<512, 2><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
   else chain_kernel<256, 3><<<n_jobs, threads, plan.bytes, stream>>>(d_jobs);
   return cudaGetLastError();
+}
+
+const void* serve_kernel_fn() { return (const void*)serve_kernel; }
+
+cudaError_t serve_prepare(int smem, int* blocks_per_sm) {
+  if (smem > kPoolMaxSmem) return cudaErrorInvalidValue;
+  static std::atomic<uint64_t> configured;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = uint64_t(1) << (dev & 63);
+  if (!(configured.load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPoolMaxSmem);
+    if (e != cudaSuccess) return e;
+    configured.fetch_or(bit, std::memory_order_release);
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_kernel, kServeThreads, smem);
+}
+
+const void* pool_kernel_fn(int cta_threads) {
+  return cta_threads > 256 ? (const void*)pool_kernel<512, 2> : (const void*)pool_kernel<256, 3>;
+}
+
+cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm) {
+  if (smem > kPoolMaxSmem || (cta_threads != 256 && cta_threads != 512)) return cudaErrorInvalidValue;
+  static std::atomic<uint64_t> configured[2];
+  const bool wide = cta_threads > 256;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = uint64_t(1) << (dev & 63);
+  if (!(configured[wide].load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(pool_kernel_fn(cta_threads), cudaFuncAttributeMaxDynamicSharedMemorySize, kPoolMaxSmem);
+    if (e != cudaSuccess) return e;
+    configured[wide].fetch_or(bit, std::memory_order_release);
+  }
+  return wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<512, 2>, cta_threads, smem)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<256, 3>, cta_threads, smem);
 }
 
 cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat, Key key,

@@ -115,4 +115,19 @@ __device__ __forceinline__ uint32_t bytesum(uint32_t w) { return (w * 0x01010101
 // 4 bits -> 4 bytes (bit b to bit 0 of byte b).
 __device__ __forceinline__ uint32_t spread4(uint32_t x) { return ((x & 0xFu) * 0x00204081u) & 0x01010101u; }
 
+// Barrier of the T threads that run one resident chain.  A chain owns the
+// whole CTA (T == blockDim.x: __syncthreads), one warp (T == 32: the lanes
+// synchronise and order their shared-memory accesses with __syncwarp), or a
+// warp-aligned group of T = 64..512 threads of a larger CTA (named barrier
+// 1 + threadIdx.x / T; at most 15 such groups per CTA).
+__device__ __forceinline__ void chain_sync(int T) {
+  if (T == (int)blockDim.x) {
+    __syncthreads();
+  } else if (T == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)threadIdx.x / T), "r"(T) : "memory");
+  }
+}
+
 }  // namespace mcrg

@@ -2,12 +2,33 @@
 // translation units of libmcrg.  Not part of the public ABI.
 #pragma once
 #include <cstdint>
+#include <utility>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/mcrg.h"
 #include "mcrg_device.cuh"
 
 namespace mcrg {
+
+// Device memory of a context: from cudaMalloc (span == nullptr), or -- for
+// the contexts a server runs its HBM-path requests on -- carved out of a
+// span of the server's arena that was reserved, and charged to its budget,
+// when the request was admitted.  Span allocations are 256-byte aligned and
+// bump-allocated; a release frees space once everything allocated after it
+// is released as well (temporaries of one call are released in reverse
+// order); the span goes back to the arena as a whole.
+struct DevSpan {
+  uint8_t* base = nullptr;
+  size_t cap = 0, used = 0;
+  std::vector<std::pair<size_t, size_t>> live;  // (offset, bytes) in allocation order; bytes 0 once released
+};
+cudaError_t dev_alloc(DevSpan* s, void** p, size_t bytes);
+void dev_release(DevSpan* s, void* p);
+template <class T>
+inline cudaError_t dev_alloc(DevSpan* s, T** p, size_t bytes) {
+  return dev_alloc(s, reinterpret_cast<void**>(p), bytes);
+}
 
 // One independent Markov chain run shared-memory resident by one CTA.
 struct ChainJob {
@@ -37,7 +58,7 @@ struct SmemPlan {
   int s_off;    // int32 S[(MCRG_MAX_LEVELS+1) * MCRG_MAX_COUPLINGS]
   int tab_off;  // int2 per moment entry: (x | y << 16, output index)
   int acc_off;  // int64 per moment entry
-  int scr_off;  // uint32 open-site scratch: 64 per warp, up to 8 warps
+  int scr_off;  // uint32 open-site scratch: 64 per warp of the chain (at least 8 warps)
   int E;        // moment entries of the T-matrix moments
   int Ecap;     // entries the table holds (also fits the 2 (n_levels + 1) flow moments)
   int qn_off;   // planes: int qn[2] (padded to 16 bytes)
@@ -55,7 +76,8 @@ __host__ __device__ inline bool resident_fits(int L, bool fast) {
   return L <= (fast ? MCRG_RESIDENT_MAX_L : MCRG_SMEM_MAX_L);
 }
 
-__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bool planes = false, bool cluster = false) {
+__host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bool planes = false, bool cluster = false,
+                                             int threads = 256) {
   SmemPlan p;
   int off = 0, n = L;
   for (int l = 0; l <= n_levels; ++l, n >>= 1) {
@@ -71,7 +93,7 @@ __host__ __device__ inline SmemPlan make_plan(int L, int n_levels, int C = 0, bo
   p.acc_off = off;
   off += p.Ecap * 8;
   p.scr_off = off;
-  off += 8 * 64 * 4;
+  off += (threads > 256 ? threads / 32 : 8) * 64 * 4;  // kOpenPerWarp words per warp of the chain
   p.qn_off = p.q_off = -1;
   if (planes) {
     off = (off + 15) / 16 * 16;  // the queue holds uint4 entries
@@ -107,6 +129,68 @@ Accept make_accept(double K);
 cudaError_t launch_chain(const ChainJob* d_jobs, int n_jobs, int L, int n_levels, int C, int threads, bool planes,
                          cudaStream_t stream, bool cluster = false);
 
+// Persistent batch (pool_kernel, mcrg_chain.cu): packs of chains taken in
+// queue order by the CTAs of one launch.  A pack is `count` chains (jobs
+// first .. first+count-1) of `threads` threads each (a multiple of 32; 32,
+// or 64 .. CTA width for named barriers), `stride` bytes of shared memory
+// each; count * threads <= CTA width and count * stride <= the launch's
+// dynamic shared memory.
+constexpr int kPoolMaxGroups = 16;
+constexpr int kPoolMaxSmem = 224 * 1024;  // dynamic shared memory per CTA (the kernel adds ~3 KB of its own)
+struct PoolPack {
+  int32_t first;
+  int16_t count;
+  int16_t threads;
+  int32_t stride;
+  int32_t pad;
+};
+struct PoolQueue {
+  int32_t n_packs;
+  int32_t pad;
+  const PoolPack* packs;
+  const ChainJob* jobs;
+  unsigned* next;  // packs handed out so far; zero before the launch
+};
+// Served requests (serve_kernel, mcrg_chain.cu): a ring of packs in page-
+// locked host memory that the server's scheduler fills and the persistent
+// CTAs drain.  Entry k lives in slot k % cap; the host writes it, then
+// publishes it by a release store of `tail` = k + 1; a CTA claims the next
+// entry with a compare-and-swap of the device counter `head` after an
+// acquire load of `tail`, runs its chains (the moments go to the jobs' bins,
+// page-locked host memory) and stores done[k % cap] = k + 1 with release
+// semantics.  A CTA with nothing to claim polls with growing sleeps and
+// leaves after `idle_ns`; the CTAs with blockIdx.x >= gridDim.x - shrink
+// leave at their next claim (space for HBM-path kernels); all leave at stop.
+struct ServeEntry {
+  PoolPack pk;  // pk.first unused: the jobs are inline
+  ChainJob jobs[kPoolMaxGroups];
+};
+struct ServeCtl {
+  unsigned long long tail;
+  unsigned long long idle_ns;
+  int32_t stop;
+  int32_t shrink;
+};
+struct ServeArgs {
+  const ServeEntry* ring;   // device address of the host ring
+  ServeCtl* ctl;            // device address of the host control block
+  unsigned int* done;       // device address of the host completion words
+  unsigned long long* head; // device memory: entries claimed so far
+  uint32_t cap;
+  uint32_t pad;
+};
+constexpr int kServeThreads = 512;
+const void* serve_kernel_fn();
+// Shared-memory limit of the serve kernel (once per device); its resident
+// CTAs per SM for `smem` bytes.
+cudaError_t serve_prepare(int smem, int* blocks_per_sm);
+
+// CTA widths of the pool kernel: 256 (3 CTAs per SM by registers) or 512.
+const void* pool_kernel_fn(int cta_threads);
+// Sets the kernel's shared-memory limit (once per device) and returns its
+// resident CTAs per SM for `smem` bytes of dynamic shared memory.
+cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm);
+
 // Stateless helpers on a device lattice in split layout (used by
 // mcrg_block_lattice / mcrg_lattice_couplings and the HBM path's tail).
 cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat,
@@ -128,6 +212,13 @@ uint32_t bond_threshold(double K);
 
 // New chain on an HBM-resident context without allocating (mcrg_capi.cu).
 int reinit_context(mcrg_ctx* c, double K, uint64_t seed, uint32_t replica);
+// mcrg_alloc with every device buffer of the context's lifetime taken from
+// `span` (nullptr: cudaMalloc).
+int context_create(mcrg_ctx** out, const mcrg_cfg* cfg, DevSpan* span);
+// Upper bound of the span bytes a context needs for mcrg_sweep / mcrg_measure
+// of n_samples (update == 0) or mcrg_cluster_update / mcrg_measure_cluster
+// (update != 0).
+size_t context_bytes(int L, int n_levels, int C, int update, int64_t n_samples);
 
 // Forward pass of the RG neural network (src/rgnn.cpp:281-307) on a split
 // layout lattice of side n: the scalar output into *d_out (device), using

@@ -413,8 +413,6 @@ __device__ __forceinline__ void reduce_into(int (&acc)[5], int* S, int C) {
   }
 }
 
-__device__ __forceinline__ void sync_group() { __syncthreads(); }
-
 
 }  // namespace
 }  // namespace mcrg

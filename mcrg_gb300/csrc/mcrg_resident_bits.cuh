@@ -212,14 +212,14 @@ __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_
     }
     Cc[r] = nt;
   }
-  __syncthreads();
+  chain_sync(T);
   const int nq = min(qn[c], cap);
   for (int e = tid; e < nq; e += T) {
     const uint4 en = q[e];
     const uint32_t fl = open_flips(key, rep, a, c, (int)en.z, (int)en.w, en.x, en.y, t);
     if (fl) Cc[(size_t)en.z * wpr + en.w] ^= fl;  // one entry per word: no two threads touch the same word
   }
-  __syncthreads();
+  chain_sync(T);
 }
 
 // One sweep: colour 0, then colour 1 (qn[0..1] zero on entry and on return).

@@ -157,7 +157,7 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
         }
       }
     }
-    __syncthreads();
+    chain_sync(T);
     for (int u = warp; u < units; u += nw) {
       const int i = u / segs, sg = u - i * segs, j0 = sg * 32, in = (i + 1) & m;
       const uint32_t vv = vb[u], hr = hb[u], hn = hb[in * segs + sg];
@@ -167,7 +167,7 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
     }
   } else {
     for (int x = tid; x < n; x += T) lab[x] = (uint16_t)x;
-    __syncthreads();
+    chain_sync(T);
     // open bonds of site pairs (i, j0), (i, j0 + 1): one Philox block each
     for (int y = tid; y < n / 2; y += T) {
       const int i = y / half, j0 = 2 * (y - i * half), id = (i + 1) & m, x0 = i * L + j0;
@@ -179,9 +179,9 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
       if (r.w < tb && lv.spin(id, j0 + 1) == s1) unite16(lab, x0 + 1, id * L + j0 + 1);
     }
   }
-  __syncthreads();
+  chain_sync(T);
   for (int x = tid; x < n; x += T) lab[x] = (uint16_t)find16(lab, x);  // flatten: every label at its root
-  __syncthreads();
+  chain_sync(T);
   if (wolff) {
     if (tid == 0) {
       const uint4 r = stream_block(key, rep, P_CLUSTER, 0u, 0u, 0u, t);
@@ -193,7 +193,7 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
           (stream_block(key, rep, P_CLUSTER, 1u, (uint32_t)x >> 16, (uint32_t)x & 0xFFFFu, t).x & 1u))
         atomicOr(&coin[x >> 5], 1u << (x & 31));
   }
-  __syncthreads();
+  chain_sync(T);
 }
 
 // Whether site x flips, after update() has labelled the level (labels flattened).
@@ -215,7 +215,7 @@ __device__ __forceinline__ void update_bytes(uint8_t* lat, int L, uint8_t* work,
       const int i = x / L, j = x - i * L;
       lat[(size_t)((i + j) & 1) * L * h + (size_t)i * h + (j >> 1)] ^= 1u;
     }
-  __syncthreads();
+  chain_sync(T);
 }
 
 // One cluster update of a plane level 0 (L >= 64): one thread per plane word.
@@ -231,7 +231,7 @@ __device__ __forceinline__ void update_planes(uint32_t* pl, int L, uint8_t* work
       if (flips(work, L, i * L + 2 * (32 * w + p) + q, wolff)) mask |= 1u << planes::plane_pos(p);
     pl[x] ^= mask;
   }
-  __syncthreads();
+  chain_sync(T);
 }
 
 }  // namespace rcluster

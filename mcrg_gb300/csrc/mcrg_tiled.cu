@@ -233,7 +233,8 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
     if (t->sms <= 0) t->sms = 1;
   }
   const size_t LL = (size_t)L * L;
-  if (cudaMalloc(&t->buf[0], LL) != cudaSuccess || cudaMalloc(&t->buf[1], LL) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(t->span, &t->buf[0], LL) != cudaSuccess || dev_alloc(t->span, &t->buf[1], LL) != cudaSuccess)
+    return MCRG_ENOMEM;
   // blocked levels 1 .. min(lt, nl)
   const int lt = first_tail_level(L);
   size_t off = 0;
@@ -242,10 +243,11 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
     off += (size_t)(L >> l) * (L >> l);
   }
   t->n_hbm = lt;
-  if (off && cudaMalloc(&t->levels, off) != cudaSuccess) return MCRG_ENOMEM;
-  if (cudaMalloc(&t->d_S, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) != cudaSuccess)
+  if (off && dev_alloc(t->span, &t->levels, off) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(t->span, &t->d_S, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS) !=
+      cudaSuccess)
     return MCRG_ENOMEM;
-  if (cudaMalloc(&t->d_status, sizeof(int)) != cudaSuccess) return MCRG_ENOMEM;
+  if (dev_alloc(t->span, &t->d_status, sizeof(int)) != cudaSuccess) return MCRG_ENOMEM;
   cudaMemsetAsync(t->d_S, 0, sizeof(unsigned long long) * (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS, s);
   cudaMemsetAsync(t->d_status, 0, sizeof(int), s);
   for (int v = 0; v < kNumVariants; ++v)
@@ -272,12 +274,12 @@ int tiled_reinit(TiledLattice* t, Key key, uint32_t replica, const Accept& acc, 
 }
 
 void tiled_free(TiledLattice* t) {
-  cudaFree(t->buf[0]);
-  cudaFree(t->buf[1]);
-  cudaFree(t->levels);
-  cudaFree(t->d_S);
-  cudaFree(t->d_status);
-  cudaFree(t->d_bins);
+  dev_release(t->span, t->d_bins);
+  dev_release(t->span, t->d_status);
+  dev_release(t->span, t->d_S);
+  dev_release(t->span, t->levels);
+  dev_release(t->span, t->buf[1]);
+  dev_release(t->span, t->buf[0]);
   *t = TiledLattice();
 }
 
@@ -396,10 +398,10 @@ int tiled_measure(TiledLattice* t, uint32_t t0, uint32_t n0, int64_t n_samples, 
                   int64_t bin_size, int64_t* n_bins, cudaStream_t s, bool flow) {
   const int64_t nb = (n_samples + bin_size - 1) / bin_size;
   if (nb > t->bins_cap) {
-    cudaFree(t->d_bins);
+    dev_release(t->span, t->d_bins);
     t->d_bins = nullptr;
     t->bins_cap = 0;
-    if (cudaMalloc(&t->d_bins, sizeof(mcrg_moments) * (size_t)nb) != cudaSuccess) return MCRG_ENOMEM;
+    if (dev_alloc(t->span, &t->d_bins, sizeof(mcrg_moments) * (size_t)nb) != cudaSuccess) return MCRG_ENOMEM;
     t->bins_cap = nb;
   }
   if (cudaMemsetAsync(t->d_bins, 0, sizeof(mcrg_moments) * (size_t)nb, s) != cudaSuccess) return MCRG_EIO;

@@ -20,6 +20,7 @@ struct TiledLattice {
   int64_t bins_cap = 0;
   int variant = -1;                       // sweep variant picked by the autotuner
   int sms = 0;                            // multiprocessors of the lattice's device
+  DevSpan* span = nullptr;                // where the buffers come from (nullptr: cudaMalloc)
 };
 
 int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica, const Accept& acc,

@@ -252,10 +252,11 @@ def test_batch_equals_single_contexts(M, use_graph):
 
 @pytest.mark.parametrize("L,C,nl", [(64, 3, -1), (128, 5, 2), (256, 4, -1), (512, 5, -1), (1024, 2, -1),
                                     (1024, 5, 4)])
-def test_batch_resident_planes_matches_oracle(M, L, C, nl):
+def test_batch_resident_planes_matches_oracle(M, L, C, nl, monkeypatch):
     """Fast-regime chains up to MCRG_RESIDENT_MAX_L run shared-memory resident, every level
     of side >= 64 as bit planes (sweeps, coupling sums and blocking on planes): the moments
     equal the oracle's chain, bin for bin."""
+    monkeypatch.setenv("MCRG_BATCH_SCHEDULE", "resident")
     nlv = int(math.log2(L)) - 1 if nl < 0 else nl
     reqs = [M.make_request(L, K, seed=40 + i, replica=i, n_eq=3, n_samples=3, sweeps_between=1 + i % 2,
                            n_levels=nl, n_couplings=C) for i, K in enumerate((KC, -0.47))]
