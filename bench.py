@@ -1,23 +1,40 @@
 """Benchmark of the MCRG Monte-Carlo / block-spin hot path on GB300.
 
-Default workload ("large"): one L = 16384 periodic 2D Ising lattice
-(268M int8 spins, HBM-resident), K = -0.4406868, 13 RG levels (b = 2
-majority rule), 5 couplings.  One step = `--sweeps-per-step` fused
+Default line (the headline workload, "large"): one L = 16384 periodic 2D
+Ising lattice (268M int8 spins, HBM-resident), K = -0.4406868, 13 RG levels
+(b = 2 majority rule), 5 couplings.  One step = `--sweeps-per-step` fused
 checkerboard sweeps + one full measurement (blocking of every level,
-coupling sums, exact int128 moment products).  Metric: Gflips/s =
-L^2 * sweeps / s (site updates).  The lattice (268 MB) is larger than L2
-(129 MB), so no L2 flush is needed between steps.
+coupling sums, exact int128 moment products).  Metric: Gflips/s = L^2 *
+sweeps / s (site updates).  The lattice (268 MB) is larger than L2 (129 MB),
+so no L2 flush is needed between steps.
 
-Other workloads (--workload): "batched" (4096 replicas, L from
-{16..256}, one launch per side, CUDA graph), "plain" (one L = 64 lattice,
-one CTA per launch), "served" (Poisson arrivals into mcrg_server).
+The same line carries, at N = 1, three sub-objects measured in the same run,
+each with its own clock record:
+  "batched": 4096 replicas in one persistent launch (L from {16..256} with
+             p = .3/.3/.2/.15/.05, K on 33 points in [-0.49, -0.43], 1e5
+             sweeps each, measured after every sweep) against the plain
+             one-lattice-per-launch path on the same requests;
+  "served":  Poisson arrivals at 1e1 .. 1e4 / s into the device-resident
+             request loop (L log-uniform in {8..1024}, K ~ U[-0.50, -0.42],
+             sweeps log-uniform in [1e3, 1e5]), p50 / p99 latency and
+             solves/s, against the plain path on the same mix;
+  "config1": the reference's CPU-runnable solve (L = 8, 1e4 + 1e5 sweeps, 2
+             levels) as MCRG solves/s: plain GPU, batched GPU, and the
+             reference's Wolff path on every host core.
+
+Other workloads (--workload): "batched", "served", "plain" (one L = 64
+lattice, one CTA per launch), "cluster" (Wolff / Swendsen-Wang updates of one
+lattice), each printed as its own line.
 
 --impl reference times the reference's CPU path (its Wolff update +
 calc_interactions + block_spin_transformation sample loop, restated in
-oracle/) on the host cores for the same workload.
+oracle/) on the host cores for the same workload and config.
 
-Multi-GPU: replicas only (each rank runs its own chain, replica = rank);
-value = all ranks' flips / max-over-ranks time.
+Multi-GPU: replicas only.  --gpus N > 1 re-launches the script under
+torch.distributed.run with N ranks; rank r runs replica r on GPU LOCAL_RANK,
+the ranks' exact moment sums are added (as MPI_Allreduce does in the
+reference, src/mcrg.cpp:101-103), and value = all ranks' flips / the slowest
+rank's time.
 """
 from __future__ import annotations
 
@@ -75,6 +92,23 @@ class Dist:
         t = torch.tensor([x], dtype=torch.float64)
         self.pg.all_reduce(t)
         return float(t.item())
+
+
+def replica_sum(m):
+    """Exact sum of every rank's moment sums (MomentSums), as MPI_Allreduce(SUM)
+    combines the ranks' chains in the reference (src/mcrg.cpp:101-103); the
+    identity on one process."""
+    from mcrg_gb300.dist import allreduce_moments
+    return allreduce_moments(m)
+
+
+def relaunch_multi(n: int) -> int:
+    """--gpus N without a launcher: run this script under torch.distributed.run
+    with N ranks on this node and return its exit code."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(29500 + os.getpid() % 1000),
+           os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
 
 
 # ---------------------------------------------------------------------------
@@ -159,6 +193,14 @@ def profiled_traffic(name: str):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
+def large_config(args, world: int) -> dict:
+    L, spp, C_ = args.L, args.sweeps_per_step, args.couplings
+    return {"workload": "large: L=%d periodic 2D Ising, K=-0.4406868, %d RG levels b=2, %d couplings, "
+                        "%d sweeps + 1 measurement per step" % (L, int(math.log2(L)) - 1, C_, spp),
+            "L": L, "K": KC, "levels": int(math.log2(L)) - 1, "couplings": C_, "sweeps_per_step": spp,
+            "parallelism": "replicas x%d" % world, "l2": "inputs larger than L2 (268 MB lattice)"}
+
+
 def run_large(args, D: Dist) -> dict:
     import torch
     import mcrg_gb300 as M
@@ -191,6 +233,7 @@ def run_large(args, D: Dist) -> dict:
     clocks = clk.stop()
     ms_max = D.max(ms)
     value = D.world * flips_per_step * args.steps / (ms_max * 1e-3) / 1e9
+    tot = replica_sum(tot)  # every rank's chain, summed exactly
 
     # ---- dominant kernel alone: the fused sweep, per launch
     n_sw = max(8, spp)
@@ -233,10 +276,7 @@ def run_large(args, D: Dist) -> dict:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (Philox-seeded initial spins; no dataset involved)",
-        "config": {"workload": "large: L=16384 periodic 2D Ising, K=-0.4406868, 13 RG levels b=2, "
-                               "%d couplings, %d sweeps + 1 measurement per step" % (C_, spp),
-                   "L": L, "K": KC, "levels": int(math.log2(L)) - 1, "couplings": C_, "sweeps_per_step": spp,
-                   "parallelism": "replicas x%d" % D.world, "l2": "inputs larger than L2 (268 MB lattice)"},
+        "config": large_config(args, D.world),
         "e2e": {"value": round(e2e, 2), "unit": "Gflips/s", "h2d_bytes_per_step": L * L,
                 "d2h_bytes_per_step": C.sizeof(_abi.Moments)},
         "gpu_launches": launches,
@@ -246,6 +286,7 @@ def run_large(args, D: Dist) -> dict:
                      "alg_bytes_per_launch": int(alg_bytes), "ms_per_launch": round(sweep_ms, 4)},
         "clocks": clocks,
         "moments_samples": tot.n_samples,
+        "samples_per_s": round(D.world * args.steps / (ms_max * 1e-3), 2),
     }
 
 
@@ -262,65 +303,215 @@ def batched_requests(M, n, sweeps, rank=0, seed0=1, update="metropolis"):
             for i, L in enumerate(Ls)]
 
 
-def run_batched(args, D: Dist) -> dict:
-    """4096 replicas in one batched call vs the same requests one lattice per launch."""
+def time_plain(M, r, device):
+    """One request on the plain GPU path: its own context and launches (mcrg_alloc,
+    mcrg_sweep / mcrg_cluster_update, mcrg_measure / mcrg_measure_cluster, mcrg_free).
+    Returns (seconds, moments)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat = M.Lattice(r.L, r.K, seed=r.seed, replica=r.replica, n_couplings=r.n_couplings, device=device)
+    if r.flags == 0:
+        lat.sweep(r.n_eq)
+        tot, _ = lat.measure(r.n_samples, r.sweeps_between)
+    else:
+        kind = "wolff" if r.flags == 1 else "sw"
+        lat.cluster_update(r.n_eq, kind)
+        tot, _ = lat.measure_cluster(r.n_samples, r.sweeps_between, kind)
+    lat.close()
+    return time.perf_counter() - t0, tot
+
+
+def plain_by_side(M, reqs, results, device, per_side: int, weights=None) -> dict:
+    """The plain one-lattice-per-launch path on `per_side` requests of every side
+    in the mix (the same requests, seeds included).  Its solves/s on the whole mix
+    is 1 / (expected seconds per request), the per-side means weighted by the
+    side's share of the mix (or `weights`).  Each plain result is compared with
+    the batched / served result of the same request (same seed: the same chain)."""
+    import numpy as np
+    by = {}
+    for i, r in enumerate(reqs):
+        by.setdefault(int(r.L), []).append(i)
+    secs, identical, n = {}, True, 0
+    for L in sorted(by):
+        ts = []
+        for i in by[L][:per_side]:
+            dt, tot = time_plain(M, reqs[i], device)
+            ts.append(dt)
+            n += 1
+            if results is not None:
+                identical &= (M.moments_from_c(results[i].moments) == tot)
+        secs[L] = float(np.mean(ts))
+    w = weights or {L: len(v) / len(reqs) for L, v in by.items()}
+    expect = sum(w[L] * secs[L] for L in secs)
+    return {"solves_per_s": round(1.0 / expect, 4), "seconds_per_request": {str(L): round(v, 4) for L, v in secs.items()},
+            "requests_timed": n, "moments_identical_to_plain": bool(identical)}
+
+
+def batched_cfg(args, D: Dist) -> dict:
+    """Config "batched": 4096 replicas in one persistent launch (graph re-launched),
+    --batch-sweeps sweeps each, measured after every sweep; --batch-steps timed runs."""
+    import numpy as np
     import torch
     import mcrg_gb300 as M
 
-    torch.cuda.set_device(D.local)
+    dev = D.local
+    torch.cuda.set_device(dev)
     reqs = batched_requests(M, args.replicas, args.batch_sweeps, D.rank, update=args.update)
-    flips = float(sum(r.L * r.L for r in reqs)) * args.batch_sweeps
     creqs = (M._abi.Request * len(reqs))(*reqs)
-    for _ in range(args.warmup):
-        M.batch_run(creqs, device=D.local, raw=True)
+    # warm-up: the same shapes with 100 samples (schedule trials, graph instantiation)
+    short = (M._abi.Request * len(reqs))(*[M.make_request(r.L, r.K, seed=r.seed, replica=r.replica, n_samples=100,
+                                                          n_couplings=r.n_couplings, update=args.update)
+                                            for r in reqs])
+    M.batch_run(short, device=dev, raw=True)
+    clk = Clocks(dev)
+    clk.start()
     D.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        M.batch_run(creqs, device=D.local, raw=True)
+    res = None
+    for _ in range(args.batch_steps):
+        res = M.batch_run(creqs, device=dev, raw=True)
     torch.cuda.synchronize()
     dt = D.max(time.perf_counter() - t0)
-    value = D.world * flips * args.steps / dt / 1e9
-    solves = D.world * len(reqs) * args.steps / dt
-    plain = run_plain_subset(M, reqs[: args.plain_subset], D.local, args.update)
-    if args.update != "metropolis":  # cluster updates: chain samples (one update + one measurement) per second
-        value = D.world * len(reqs) * args.batch_sweeps * args.steps / dt / 1e6
-        metric = unit = "Msamples/s"
-    else:
-        metric = unit = "Gflips/s"
-    return {"metric": metric, "value": round(value, 2), "unit": unit, "n_gpus": D.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-            "data": "synthetic", "solves_per_s": round(solves, 1),
+    clocks = clk.stop()
+    assert all(r.status == 0 for r in res)
+    lat = np.array([r.done_s - r.submit_s for r in res])
+    flips = float(sum(r.L * r.L for r in reqs)) * args.batch_sweeps
+    solves = D.world * len(reqs) * args.batch_steps / dt
+    plain = plain_by_side(M, reqs, res, dev, args.plain_per_side)
+    sched = {}
+    for L in (16, 32, 64, 128, 256):
+        sc = M.batch_schedule(M.make_request(L, -0.46, seed=1, n_samples=10, n_couplings=2), dev)
+        sched[str(L)] = sc["threads"]
+    st = M.batch_stats(dev)
+    return {"solves_per_s": round(solves, 2), "Gflips_per_s": round(D.world * flips * args.batch_steps / dt / 1e9, 2),
+            "seconds_per_batch": round(dt / args.batch_steps, 3),
+            "p50_latency_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_latency_s": round(float(np.percentile(lat, 99)), 4),
             "plain": plain, "batched_over_plain_solves": round(solves / D.world / plain["solves_per_s"], 1),
-            "config": {"workload": "batched: %d replicas, L in {16..256} (p = .3/.3/.2/.15/.05), K on 33 points in "
-                                   "[-0.49,-0.43], %d %s each, measured after every one, 2 couplings"
-                                   % (args.replicas, args.batch_sweeps,
-                                      "sweeps" if args.update == "metropolis" else args.update + " updates"),
-                       "parallelism": "replicas x%d" % D.world,
-                       "equal_error": "batched and one-per-launch runs give bit-identical moment sums per seed"}}
+            "equal_error": "same seeds: batched and plain runs give bit-identical moment sums, so identical "
+                           "T-eigenvalue estimates and error bars (checked on the timed plain requests)",
+            "threads_per_chain": sched, "graph_builds": st["graph_builds"], "launches": st["launches"],
+            "clocks": clocks,
+            "config": {"workload": "batched: %d replicas in one persistent launch, L in {16..256} (p = .3/.3/.2/.15/"
+                                   ".05), K on 33 points in [-0.49,-0.43], %d %s each measured after every one, "
+                                   "log2(L)-1 levels b=2, 2 couplings; %d timed batches"
+                                   % (len(reqs), args.batch_sweeps,
+                                      "sweeps" if args.update == "metropolis" else args.update + " updates",
+                                      args.batch_steps),
+                       "plain": "one lattice per launch on %d requests of each side, weighted by the mix"
+                                % args.plain_per_side}}
 
 
-def run_plain_subset(M, reqs, device, update="metropolis") -> dict:
-    """The plain GPU path: each request alone, one lattice per launch
-    (mcrg_alloc, mcrg_sweep / mcrg_cluster_update, mcrg_measure / mcrg_measure_cluster,
-    mcrg_free), back to back."""
+def served_requests(M, rng, n, seed0, scale=1.0):
+    """Config "served": L log-uniform in {8..1024}, K ~ U[-0.50, -0.42], sweeps
+    log-uniform in [1e3, 1e5] (times `scale`), measured after every sweep, log2(L)-1
+    levels, 2 couplings, a seed per request."""
+    import numpy as np
+    Ls = 2 ** rng.integers(3, 11, size=n)
+    Ks = rng.uniform(-0.50, -0.42, size=n)
+    sw = np.maximum(1, (np.exp(rng.uniform(np.log(1e3), np.log(1e5), size=n)) * scale).astype(np.int64))
+    return [M.make_request(int(L), float(K), seed=seed0 + i, replica=i, n_eq=0, n_samples=int(s_),
+                           sweeps_between=1, n_couplings=2) for i, (L, K, s_) in enumerate(zip(Ls, Ks, sw))]
+
+
+def served_cfg(args, D: Dist) -> dict:
+    """Poisson arrivals into the device-resident request loop at 1e1, 1e2, 1e3 and
+    1e4 requests/s (about two seconds of arrivals each, 40 .. --served-requests
+    requests), each rate drained before the next.  The headline is the solves/s at
+    the highest rate (the server's capacity)."""
+    import numpy as np
     import torch
+    import mcrg_gb300 as M
+
+    dev = D.local
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(11 + D.rank)
+    for L in (8, 16, 32, 64, 128, 256, 512, 1024):  # schedule trials before the server runs
+        M.batch_schedule(M.make_request(L, -0.46, seed=1, n_samples=10, n_couplings=2), dev)
+    srv = M.Server(device=dev, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)),
+                   hbm_workers=args.served_hbm_workers)
+    rates, mix, results = {}, [], []
+    clk = Clocks(dev)
+    clk.start()
+    try:
+        for k, rate in enumerate((1e1, 1e2, 1e3, 1e4)):
+            n = int(min(args.served_requests, max(40, 2 * rate)))
+            reqs = served_requests(M, rng, n, 100 + 100000 * k, args.served_scale)
+            gaps = rng.exponential(1.0 / rate, size=n)
+            t0 = time.perf_counter()
+            tickets = []
+            target = t0
+            for r, g in zip(reqs, gaps):
+                target += g
+                while time.perf_counter() < target:
+                    pass
+                tickets.append(srv.submit(r))
+            out = [srv.wait(t, 900) for t in tickets]
+            wall = time.perf_counter() - t0
+            assert all(o.status == 0 for o in out)
+            lat = np.array([o.done_s - o.submit_s for o in out])
+            flips = float(sum(r.L * r.L * r.n_samples for r in reqs))
+            rates["%.0f/s" % rate] = {"requests": n, "solves_per_s": round(n / wall, 2),
+                                      "p50_latency_s": round(float(np.percentile(lat, 50)), 4),
+                                      "p99_latency_s": round(float(np.percentile(lat, 99)), 4),
+                                      "Gflips_per_s": round(flips / wall / 1e9, 2), "wall_s": round(wall, 3)}
+            mix += reqs
+            results += out
+        loop = srv.loop_stats()
+    finally:
+        srv.close()
+    clocks = clk.stop()
+    top = rates["10000/s"]
+    # the plain path on the same mix: every side equally likely (the config's log-uniform L)
+    plain = plain_by_side(M, mix, results, dev, args.plain_per_side, weights={2 ** e: 1 / 8 for e in range(3, 11)})
+    return {"solves_per_s": top["solves_per_s"], "p50_latency_s": top["p50_latency_s"],
+            "p99_latency_s": top["p99_latency_s"], "rates": rates, "plain": plain,
+            "served_over_plain_solves": round(top["solves_per_s"] / plain["solves_per_s"], 1),
+            "loop": loop, "clocks": clocks,
+            "equal_error": "same seeds: served and plain runs give bit-identical moment sums (checked on the timed "
+                           "plain requests)",
+            "config": {"workload": "served: Poisson arrivals at 1e1, 1e2, 1e3, 1e4 /s (about 2 s of arrivals each, "
+                                   "40..%d requests), L log-uniform {8..1024}, K~U[-0.50,-0.42], sweeps log-uniform "
+                                   "[1e3,1e5] x %.3g measured after every sweep, log2(L)-1 levels, 2 couplings, "
+                                   "slots %d, HBM budget %.0f GB"
+                                   % (args.served_requests, args.served_scale, args.served_slots,
+                                      args.served_budget_gb),
+                       "plain": "one lattice per launch on %d requests of each side, sides weighted equally"
+                                % args.plain_per_side}}
+
+
+def config1_cfg(args, D: Dist) -> dict:
+    """The reference's CPU-runnable solve (L = 8, K = Kc, 1e4 + 1e5 sweeps, 2 levels,
+    2 couplings) as MCRG solves/s: plain GPU (one context), batched GPU (--replicas
+    solves in one launch), the reference's path (oracle port of its Wolff step +
+    measurement) on every host core."""
+    import torch
+    import mcrg_gb300 as M
+    dev = D.local
+    torch.cuda.set_device(dev)
+    n_eq, n_s = 10000, 100000
+    r0 = M.make_request(8, KC, seed=1, n_eq=n_eq, n_samples=n_s, n_couplings=2)
+    dt_plain, _ = time_plain(M, r0, dev)
+    reqs = (M._abi.Request * args.replicas)(*[M.make_request(8, KC, seed=1 + i, replica=i, n_eq=n_eq, n_samples=n_s,
+                                                               n_couplings=2) for i in range(args.replicas)])
+    M.batch_run(reqs, device=dev, raw=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for r in reqs:
-        lat = M.Lattice(r.L, r.K, seed=r.seed, replica=r.replica, n_couplings=r.n_couplings, device=device)
-        if update == "metropolis":
-            lat.sweep(r.n_eq)
-            lat.measure(r.n_samples, r.sweeps_between)
-        else:
-            lat.cluster_update(r.n_eq, update)
-            lat.measure_cluster(r.n_samples, r.sweeps_between, update)
-        lat.close()
-    dt = time.perf_counter() - t0
-    flips = float(sum(r.L * r.L * (r.n_eq + r.n_samples * r.sweeps_between) for r in reqs))
-    return {"solves_per_s": round(len(reqs) / dt, 2), "Gflips_per_s": round(flips / dt / 1e9, 3),
-            "requests": len(reqs), "seconds": round(dt, 3)}
+    M.batch_run(reqs, device=dev, raw=True)
+    dt_batch = time.perf_counter() - t0
+    out = {"gpu_plain_solves_per_s": round(1 / dt_plain, 3),
+           "gpu_batched_solves_per_s": round(args.replicas / dt_batch, 1),
+           "config": {"workload": "config 1: L=8, K=Kc, 1e4 + 1e5 sweeps, 2 levels, 2 couplings; batched: %d solves "
+                                  "per launch" % args.replicas}}
+    if not args.no_cpu_baseline:
+        th = os.cpu_count() or 1
+        cpu = cpu_config1(th)
+        out["cpu_reference_solves_per_s"] = round(cpu["solves_per_s"], 3)
+        out["cpu_cores"] = th
+        out["cpu_sample"] = "%d independent reference solves (Wolff steps, oracle port), one per thread" % th
+    return out
 
 
 def run_cluster(args, D: Dist) -> dict:
@@ -390,70 +581,22 @@ def run_plain(args, D: Dist) -> dict:
                                    "sweep; step = %d sweeps (one error bin)" % args.plain_sweeps}}
 
 
+def run_batched(args, D: Dist) -> dict:
+    """--workload batched: the batched sub-object as its own line."""
+    sub = batched_cfg(args, D)
+    return {"metric": "MCRG solves/s", "value": sub["solves_per_s"], "unit": "solves/s", "n_gpus": D.world,
+            "steps": args.batch_steps, "warmup": 1, "ms_per_step": round(sub["seconds_per_batch"] * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            **{k: v for k, v in sub.items() if k not in ("solves_per_s",)}}
+
+
 def run_served(args, D: Dist) -> dict:
-    """Poisson arrivals of MCRG requests (L log-uniform in {8..1024}, K ~ U[-0.50,-0.42],
-    sweeps log-uniform in [1e3, 1e5] scaled by --served-scale) into mcrg_server, at arrival
-    rates swept over 1e1, 1e2, 1e3 and 1e4 per second (at least 50 requests, about two seconds
-    of arrivals from 1e2/s on, at most --served-requests).  The headline is the solves/s at the highest rate (the server's
-    capacity), against the plain one-lattice-per-launch path on a subset of the same mix."""
-    import numpy as np
-    import torch
-    import mcrg_gb300 as M
-    torch.cuda.set_device(D.local)
-    rng = np.random.default_rng(11 + D.rank)
-
-    def make(n, seed0):
-        Ls = 2 ** rng.integers(3, 11, size=n)
-        Ks = rng.uniform(-0.50, -0.42, size=n)
-        sw = np.exp(rng.uniform(np.log(1e3), np.log(1e5), size=n)) * args.served_scale
-        sw = np.maximum(1, sw.astype(np.int64))
-        return [M.make_request(int(L), float(K), seed=seed0 + i, replica=i, n_eq=0, n_samples=int(s_),
-                               sweeps_between=1, n_couplings=2) for i, (L, K, s_) in enumerate(zip(Ls, Ks, sw))]
-
-    rates = {}
-    all_reqs = []
-    srv = M.Server(device=D.local, slots=args.served_slots, hbm_budget_bytes=int(args.served_budget_gb * (1 << 30)),
-                   hbm_workers=args.served_hbm_workers)
-    try:
-        for rate in (1e1, 1e2, 1e3, 1e4):
-            n = int(min(args.served_requests, max(50, 2 * rate)))
-            reqs = make(n, 100 + 100000 * len(rates))
-            all_reqs += reqs
-            gaps = rng.exponential(1.0 / rate, size=n)
-            t0 = time.perf_counter()
-            tickets = []
-            for r, g in zip(reqs, gaps):
-                target = (tickets[-1][1] if tickets else t0) + g
-                while time.perf_counter() < target:
-                    pass
-                tickets.append((srv.submit(r), time.perf_counter()))
-            lat = []
-            for tk, ts in tickets:
-                res = srv.wait(tk, 600)
-                lat.append(res.done_s - res.submit_s)
-            wall = time.perf_counter() - t0
-            lat = np.array(lat)
-            flips = float(sum(r.L * r.L * r.n_samples for r in reqs))
-            rates["%.0f/s" % rate] = {"requests": n, "solves_per_s": round(n / wall, 2),
-                                      "p50_latency_s": round(float(np.percentile(lat, 50)), 4),
-                                      "p99_latency_s": round(float(np.percentile(lat, 99)), 4),
-                                      "Gflips_per_s": round(flips / wall / 1e9, 2), "wall_s": round(wall, 3)}
-    finally:
-        srv.close()
-    top = rates["10000/s"]
-    # the plain GPU path on a random subset of the same request mix (one lattice per launch, back to back)
-    sub = [all_reqs[int(i)] for i in rng.choice(len(all_reqs), size=min(len(all_reqs), args.plain_subset),
-                                                replace=False)]
-    plain = run_plain_subset(M, sub, D.local)
-    return {"metric": "MCRG solves/s", "value": top["solves_per_s"], "unit": "solves/s", "n_gpus": D.world,
-            "steps": 1, "warmup": 0, "ms_per_step": round(top["wall_s"] * 1e3, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "p50_latency_s": top["p50_latency_s"], "p99_latency_s": top["p99_latency_s"],
-            "rates": rates, "plain": plain,
-            "served_over_plain_solves": round(top["solves_per_s"] / plain["solves_per_s"], 2),
-            "config": {"workload": "served: Poisson arrivals at 1e1, 1e2, 1e3, 1e4 /s, L log-uniform {8..1024}, "
-                                   "K~U[-0.50,-0.42], sweeps log-uniform [1e3,1e5] x %.3g, slots %d, budget %.0f GB"
-                                   % (args.served_scale, args.served_slots, args.served_budget_gb)}}
+    """--workload served: the served sub-object as its own line."""
+    sub = served_cfg(args, D)
+    return {"metric": "MCRG solves/s", "value": sub["solves_per_s"], "unit": "solves/s", "n_gpus": D.world,
+            "steps": 1, "warmup": 0, "ms_per_step": round(sub["rates"]["10000/s"]["wall_s"] * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            **{k: v for k, v in sub.items() if k not in ("solves_per_s",)}}
 
 
 # ---------------------------------------------------------------------------
@@ -465,7 +608,8 @@ class RefCPU:
     replicas, each on its own OS thread (the oracle's restatement; ctypes
     releases the GIL).  Replicas start ordered and are relaxed once."""
 
-    def __init__(self, L: int, threads: int, n_couplings: int = 2, relax_steps: int = 3):
+    def __init__(self, L: int, threads: int, n_couplings: int = 2, relax_steps: int = 1):
+        import numpy as np
         from oracle import oracle as O
         self.O = O
         self.L, self.threads, self.C = L, threads, n_couplings
@@ -481,7 +625,6 @@ class RefCPU:
             w.steps(s, relax_steps)
             self.spins[k], self.wolff[k] = s, w
 
-        import numpy as np
         self._run(init)
 
     def _run(self, fn):
@@ -509,7 +652,8 @@ class RefCPU:
         t0 = time.perf_counter()
         self._run(work)
         wall = time.perf_counter() - t0
-        return {"flips_per_s": sum(r[0] for r in res) / wall, "samples": sum(r[1] for r in res), "wall_s": wall}
+        return {"flips_per_s": sum(r[0] for r in res) / wall, "flipped": sum(r[0] for r in res),
+                "samples": sum(r[1] for r in res), "wall_s": wall}
 
     def close(self):
         for w in self.wolff:
@@ -551,11 +695,81 @@ def cpu_checkerboard(seconds: float, threads: int, L: int = 1024) -> dict:
     return {"flips_per_s": sum(done) * L * L / wall, "sweeps": sum(done), "wall_s": wall, "L": L}
 
 
-def cpu_threads(L: int) -> int:
-    """All host threads, capped at 8 for L >= 8192 (each Wolff replica holds
-    ~2.3 GB of host state at L = 16384)."""
+def cpu_threads(L: int) -> tuple[int, str]:
+    """Host threads for the reference's CPU path: every core, unless the
+    replicas' host state (~2.4 GB each at L = 16384: spins, cluster marks and
+    frontier) would not fit in 60 % of the available memory."""
     n = os.cpu_count() or 1
-    return min(n, 8) if L >= 8192 else n
+    per = 2.4e9 * (L / 16384.0) ** 2
+    try:
+        with open("/proc/meminfo") as f:
+            avail = next(int(ln.split()[1]) * 1024 for ln in f if ln.startswith("MemAvailable"))
+    except Exception:
+        return n, "all %d host cores" % n
+    fit = max(1, int(0.6 * avail / per))
+    if fit >= n:
+        return n, "all %d host cores" % n
+    return fit, "%d of %d host cores: %.1f GB of host state per replica, %.0f GB available" % (
+        fit, n, per / 1e9, avail / 1e9)
+
+
+def cpu_config1(threads: int) -> dict:
+    """The reference's full CPU solve of config 1 (L = 8, 1e4 + 1e5 Wolff steps with a
+    2-level measurement after each), one independent solve per thread."""
+    from oracle import oracle as O
+    done = [0] * threads
+
+    def work(k):
+        O.wolff_chain(8, KC, 2, 2, 500 + k, 10000, 100000, trace=False)
+        done[k] = 1
+
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    return {"solves_per_s": sum(done) / wall, "wall_s": wall}
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU path (oracle port of its Wolff step +
+    all-level measurement per sample) on the machine's host cores, for the GB300 arm's
+    config; each step is one reference sample on every thread's own replica."""
+    threads, why = cpu_threads(args.L)
+    ref = RefCPU(args.L, threads, args.couplings)
+    vals = []
+    try:
+        for _ in range(args.warmup):
+            ref.step(0.0)  # one sample per thread (at least), untimed
+        for _ in range(args.steps):
+            vals.append(ref.step(0.0))
+    finally:
+        ref.close()
+    wall = sum(v["wall_s"] for v in vals)
+    fl = sum(v["flipped"] for v in vals) / wall / 1e9
+    samples = sum(v["samples"] for v in vals)
+    ck_threads = os.cpu_count() or 1
+    ck = cpu_checkerboard(min(5.0, args.cpu_seconds / 3), ck_threads)
+    return {"impl": "reference", "metric": "Gflips/s", "value": round(fl, 5), "unit": "Gflips/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(wall / max(1, args.steps) * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "i8", "data": "synthetic (ordered start relaxed by one Wolff step)",
+            "config": large_config(args, 1),
+            "flips_are": "spins flipped by the reference's Wolff update (its own update rule)",
+            "samples_per_s": round(samples / wall, 4),
+            "cpu_baseline": {"value": round(fl, 5), "unit": "Gflips/s", "cores": threads, "kind": "port",
+                             "sample": "%d independent L=%d replicas, one per thread (%s); %d timed steps of one "
+                                       "reference sample (Wolff step + %d-level measurement) per replica, %d samples "
+                                       "in %.1f s" % (threads, args.L, why, args.steps, int(math.log2(args.L)) - 1,
+                                                      samples, wall),
+                             "checkerboard_port": {
+                                 "value": round(ck["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": ck_threads,
+                                 "sample": "the oracle's Philox checkerboard sweep (the GPU's update, site updates), "
+                                           "%d independent L=%d lattices for %.1f s" % (ck_threads, ck["L"],
+                                                                                       ck["wall_s"])}},
+            "e2e": {"value": round(fl, 5), "unit": "Gflips/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -569,67 +783,58 @@ def main():
     ap.add_argument("--sweeps-per-step", type=int, default=200)
     ap.add_argument("--couplings", type=int, default=5)
     ap.add_argument("--replicas", type=int, default=4096)
-    ap.add_argument("--batch-sweeps", type=int, default=1000)
+    ap.add_argument("--batch-sweeps", type=int, default=100000)
+    ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--update", default="metropolis", choices=["metropolis", "wolff", "sw"],
                     help="update rule of the batched workload's chains (cluster workload: wolff or sw)")
     ap.add_argument("--cluster-updates", type=int, default=10, help="cluster workload: updates per step")
     ap.add_argument("--cluster-equilibrate", type=int, default=60, help="cluster workload: SW updates first")
-    ap.add_argument("--plain-subset", type=int, default=64)
+    ap.add_argument("--plain-per-side", type=int, default=2, help="plain-path requests timed per lattice side")
     ap.add_argument("--plain-sweeps", type=int, default=10000)
-    ap.add_argument("--served-requests", type=int, default=2000)
-    ap.add_argument("--served-rate", type=float, default=1000.0)
-    ap.add_argument("--served-scale", type=float, default=0.01)
-    ap.add_argument("--served-slots", type=int, default=512)
+    ap.add_argument("--served-requests", type=int, default=800)
+    ap.add_argument("--served-scale", type=float, default=1.0, help="sweeps of the served mix x this (1: as stated)")
+    ap.add_argument("--served-slots", type=int, default=1024)
     ap.add_argument("--served-budget-gb", type=float, default=150.0)
-    ap.add_argument("--served-hbm-workers", type=int, default=0, help="host threads for L > 256 requests (0: 16)")
+    ap.add_argument("--served-hbm-workers", type=int, default=0, help="host threads for HBM-path requests (0: 16)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="default workload: skip the batched / served / config1 "
+                                                          "sub-objects")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_multi(args.gpus))
     D = Dist()
 
     if args.impl == "reference":
         if D.rank != 0:
             return
-        threads = cpu_threads(args.L)
-        per = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
-        ref = RefCPU(args.L, threads)
-        vals = []
-        for _ in range(args.warmup):
-            ref.step(per / 2)
-        for _ in range(args.steps):
-            vals.append(ref.step(per))
-        ref.close()
-        fl = sum(v["flips_per_s"] for v in vals) / len(vals) / 1e9
-        out = {"impl": "reference", "metric": "Gflips/s", "value": round(fl, 4), "unit": "Gflips/s",
-               "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "i8", "data": "synthetic",
-               "config": {"workload": "large: L=%d periodic 2D Ising, K=-0.4406868 (reference Wolff update + "
-                                      "all-level measurement per sample)" % args.L},
-               "cpu_baseline": {"value": round(fl, 4), "unit": "Gflips/s", "cores": threads, "kind": "port",
-                                "sample": "%d threads x ~%.1f s of Wolff steps + measurement on L=%d replicas"
-                                          % (threads, per, args.L)},
-               "e2e": {"value": round(fl, 4), "unit": "Gflips/s", "h2d_bytes_per_step": 0,
-                       "d2h_bytes_per_step": 0}}
-        print(json.dumps(out), flush=True)
+        print(json.dumps(reference_arm(args)), flush=True)
         return
 
     out = {"large": run_large, "batched": run_batched, "plain": run_plain, "served": run_served,
            "cluster": run_cluster}[args.workload](args, D)
+    if args.workload == "large" and D.world == 1 and not args.no_sub:
+        out["batched"] = batched_cfg(args, D)
+        out["served"] = served_cfg(args, D)
+        out["config1"] = config1_cfg(args, D)
     if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline and args.workload != "cluster":
-        threads = cpu_threads(args.L)
-        cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads)
-        out["cpu_baseline"] = {"value": round(cb["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": threads,
+        threads, why = cpu_threads(args.L if args.workload == "large" else 64)
+        cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads, args.couplings)
+        out["cpu_baseline"] = {"value": round(cb["flips_per_s"] / 1e9, 5), "unit": "Gflips/s", "cores": threads,
                                "kind": "port",
-                               "sample": "reference Wolff update + measurement, %d independent replicas on %d "
-                                         "threads for %.1f s (%d samples)" % (threads, threads, cb["wall_s"],
-                                                                             cb["samples"])}
+                               "sample": "reference Wolff update + measurement, %d independent replicas (%s) for "
+                                         "%.1f s (%d samples)" % (threads, why, cb["wall_s"], cb["samples"]),
+                               "samples_per_s": round(cb["samples"] / cb["wall_s"], 4),
+                               "flips_are": "spins flipped by the reference's Wolff update"}
         ck_threads = os.cpu_count() or 1
         ck = cpu_checkerboard(min(5.0, args.cpu_seconds / 3), ck_threads)
         out["cpu_baseline"]["checkerboard_port"] = {
             "value": round(ck["flips_per_s"] / 1e9, 4), "unit": "Gflips/s", "cores": ck_threads,
-            "sample": "oracle Philox checkerboard sweeps, %d independent L=%d lattices on %d threads for %.1f s "
-                      "(%d sweeps)" % (ck_threads, ck["L"], ck_threads, ck["wall_s"], ck["sweeps"])}
+            "sample": "oracle Philox checkerboard sweeps (site updates, the GPU's work unit), %d independent L=%d "
+                      "lattices on %d threads for %.1f s (%d sweeps)" % (ck_threads, ck["L"], ck_threads,
+                                                                         ck["wall_s"], ck["sweeps"])}
+        if args.workload == "large":
+            out["gpu_over_checkerboard_port"] = round(out["value"] / (ck["flips_per_s"] / 1e9), 1)
     if D.rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -368,6 +368,10 @@ int mcrg_cancel(mcrg_server* srv, uint64_t ticket);
 int mcrg_wait(mcrg_server* srv, uint64_t ticket, double timeout_s, mcrg_result* out);
 int mcrg_server_stats(mcrg_server* srv, int64_t* admitted, int64_t* completed, int64_t* in_flight,
                       int64_t* bytes_in_use);
+/* The device-resident request loop: how many times the server launched it
+ * (it runs until no request has arrived for 20 ms) and how many packs of
+ * requests it published to it.  No counterpart in the reference. */
+int mcrg_server_loop_stats(mcrg_server* srv, int64_t* loop_launches, int64_t* entries_published);
 int mcrg_server_destroy(mcrg_server* srv);
 
 #ifdef __cplusplus

@@ -462,6 +462,12 @@ class Server:
         check(lib().mcrg_server_stats(self._h, C.byref(a), C.byref(c), C.byref(f), C.byref(b)), "mcrg_server_stats")
         return {"admitted": a.value, "completed": c.value, "in_flight": f.value, "bytes_in_use": b.value}
 
+    def loop_stats(self) -> dict:
+        """Launches of the device-resident request loop and packs published to it."""
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().mcrg_server_loop_stats(self._h, C.byref(a), C.byref(b)), "mcrg_server_loop_stats")
+        return {"loop_launches": a.value, "entries_published": b.value}
+
     def close(self):
         if getattr(self, "_h", None) is not None:
             lib().mcrg_server_destroy(self._h)

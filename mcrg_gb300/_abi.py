@@ -105,6 +105,7 @@ _SIGS = {
     "mcrg_poll": (C.c_int, [C.c_void_p, C.c_uint64, P(Result)]),
     "mcrg_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double, P(Result)]),
     "mcrg_server_stats": (C.c_int, [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)]),
+    "mcrg_server_loop_stats": (C.c_int, [C.c_void_p, P(C.c_int64), P(C.c_int64)]),
     "mcrg_server_destroy": (C.c_int, [C.c_void_p]),
 }
 

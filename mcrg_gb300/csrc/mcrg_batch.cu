@@ -171,10 +171,20 @@ std::vector<int> candidate_threads(int L, int mode) {
   return {256, 512};
 }
 
+// One timed candidate: threads per chain, seconds per sample of one chain in
+// a full wave of the trial (its latency under load), and chain samples per
+// second of the whole device running only this shape (its throughput).
+struct Candidate {
+  int threads = 0;
+  double s_sample = 0;
+  double rate = 0;
+};
+
 struct Schedule {
-  int threads = 0;       // threads per chain
-  double s_sample = 0;   // seconds per sample of one chain in a full wave of the trial
+  int threads = 0;       // threads per chain of the best-throughput candidate
+  double s_sample = 0;   // its seconds per sample of one chain in a full wave
   double s_tiled = -1;   // seconds per sample of the same chain on the HBM path (-1: not timed)
+  std::vector<Candidate> cand;  // every candidate that fits
 };
 
 std::mutex g_tune_mu;
@@ -454,6 +464,7 @@ Schedule schedule_for(BatchWorkspace& w, int device, int L, int nl, int C, int m
     pack_geometry(L, nl, C, mode, g, W, &m, &stride);
     pool_prepare(W, m * stride, &occ);
     const double rate = (double)w.sms * occ * m / t;  // chain samples per second over the device
+    best.cand.push_back(Candidate{g, t, rate});
     if (rate > best_rate) {
       best_rate = rate;
       best.threads = g;
@@ -463,12 +474,68 @@ Schedule schedule_for(BatchWorkspace& w, int device, int L, int nl, int C, int m
   if (!best.threads) {  // nothing fit (should not happen for resident shapes): the fixed rule
     best.threads = resident_threads(L, (mode & 2) != 0);
     best.s_sample = 0;
+    best.cand.push_back(Candidate{best.threads, 0.0, 0.0});
   }
   if (forced) return best;
   if (tiled_candidate(L, mode)) best.s_tiled = trial_tiled(device, L, nl, C);
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune[key] = best;
   return best;
+}
+
+// Requests of one chain shape in a batch and their packing.
+struct Shape {
+  int L, mode, nl, C, g, per_pack, stride;
+  std::vector<int> reqs;
+};
+
+// Work of a chain in sample units (a sample is one sweep or update plus one
+// measurement; a bare sweep or update counts half).
+double chain_samples(const mcrg_request& q) {
+  const double sweeps = (double)q.n_eq + (double)q.n_samples * (double)(q.sweeps_between > 1 ? q.sweeps_between - 1 : 0);
+  return (double)q.n_samples + 0.5 * sweeps;
+}
+
+// Threads per chain for every shape of a batch: the combination of timed
+// candidates with the smallest estimated makespan, max(longest chain at its
+// latency under load, total work at each shape's device throughput) -- the
+// best-throughput candidate alone can leave the batch waiting on a few long,
+// narrow chains.
+void choose_threads(std::vector<Shape>& sh, const std::vector<std::vector<Candidate>>& cands,
+                    const mcrg_request* reqs) {
+  const size_t n = sh.size();
+  double combos = 1;
+  for (auto& c : cands) combos *= (double)std::max<size_t>(c.size(), 1);
+  if (n == 0 || combos > 65536) return;  // keep each shape's best-throughput pick
+  std::vector<double> longest(n, 0), total(n, 0);
+  for (size_t k = 0; k < n; ++k)
+    for (int i : sh[k].reqs) {
+      const double w = chain_samples(reqs[i]);
+      longest[k] = std::max(longest[k], w);
+      total[k] += w;
+    }
+  std::vector<size_t> pick(n, 0), best(n, 0);
+  double best_t = -1;
+  for (;;) {
+    double lat = 0, thr = 0;
+    bool ok = true;
+    for (size_t k = 0; k < n; ++k) {
+      const Candidate& c = cands[k][pick[k]];
+      if (c.rate <= 0) ok = false;
+      lat = std::max(lat, longest[k] * c.s_sample);
+      thr += c.rate > 0 ? total[k] / c.rate : 0;
+    }
+    const double t = std::max(lat, thr);
+    if (ok && (best_t < 0 || t < best_t)) {
+      best_t = t;
+      best = pick;
+    }
+    size_t k = 0;
+    while (k < n && ++pick[k] == cands[k].size()) pick[k++] = 0;
+    if (k == n) break;
+  }
+  if (best_t < 0) return;
+  for (size_t k = 0; k < n; ++k) sh[k].g = cands[k][best[k]].threads;
 }
 
 }  // namespace
@@ -499,11 +566,8 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     std::lock_guard<std::mutex> lk(w.mu);
     rc = w.init(device);
     // schedules (autotuned once per shape), the CTA width and the packs
-    struct Shape {
-      int L, mode, nl, C, g, per_pack, stride;
-      std::vector<int> reqs;
-    };
     std::vector<Shape> sh;
+    std::vector<std::vector<Candidate>> cands;
     int W = 256;
     const char* se = getenv("MCRG_BATCH_SCHEDULE");
     const int sched_env = !se ? 0 : (!strcmp(se, "resident") ? 1 : (!strcmp(se, "tiled") ? 2 : 0));
@@ -527,9 +591,11 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         continue;
       }
       s.g = sc.threads;
-      W = std::max(W, s.g > 256 ? 512 : 256);
       sh.push_back(s);
+      cands.push_back(sc.cand);
     }
+    choose_threads(sh, cands, reqs);
+    for (auto& s : sh) W = std::max(W, s.g > 256 ? 512 : 256);
     std::vector<PoolPack> packs;
     std::vector<ChainJob> jobs;
     std::vector<int> order;  // job index -> request
@@ -539,12 +605,16 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     int64_t total_bins = 0;
     int smem = 16;
     std::vector<std::pair<double, PoolPack>> costed;
+    for (auto it = sh.begin(); it != sh.end();) {  // a shape no pack holds runs on the tiled path
+      if (!pack_geometry(it->L, it->nl, it->C, it->mode, it->g, W, &it->per_pack, &it->stride)) {
+        tiled.insert(tiled.end(), it->reqs.begin(), it->reqs.end());
+        it = sh.erase(it);
+      } else {
+        ++it;
+      }
+    }
     for (auto& s : sh) {
       if (rc) break;
-      if (!pack_geometry(s.L, s.nl, s.C, s.mode, s.g, W, &s.per_pack, &s.stride)) {
-        rc = MCRG_EINVAL;
-        break;
-      }
       auto cost = [&](int i) {
         const mcrg_request& q = reqs[i];
         return (double)q.L * q.L * (double)(q.n_eq + q.n_samples * (q.sweeps_between + 1));
@@ -643,13 +713,46 @@ extern "C" int mcrg_batch_stats(int32_t device, int64_t* launches, int64_t* grap
 // ===========================================================================
 // Server
 // ===========================================================================
+// Resident requests are published as packs into a ring in page-locked host
+// memory and run by the persistent serve kernel (mcrg_chain.cu), whose CTAs
+// claim entries as they are published and write each chain's moments into
+// page-locked host bins: admission, overlap and completion need no launch
+// per request and no copy.  The scheduler thread admits, publishes, restarts
+// the loop when it has gone idle, and retires finished entries.  Requests no
+// resident chain holds run on host worker threads, each on a context whose
+// device buffers are carved from the request's reservation in the arena.
+namespace {
+
+constexpr int kServeBinsPerChain = 4;        // host bins per resident chain (2^26 samples)
+constexpr int kHbmWorkersDefault = 16;
+constexpr int kHbmWorkersMax = 256;
+constexpr unsigned long long kServeIdleNs = 20000000ull;  // a CTA leaves after 20 ms without work
+
+struct Member {  // one admitted request
+  uint64_t ticket;
+  mcrg_request r;
+  int nl;
+  double submit_s;
+  size_t off, bytes;  // arena reservation
+  int bin_slot;       // resident: its host bins; -1: HBM path
+};
+
+struct EntryState {
+  bool busy = false;
+  uint64_t seq = 0;  // entry index + 1
+  std::vector<Member> members;
+};
+
+}  // namespace
+
 struct mcrg_server {
   mcrg_server_cfg cfg;
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_hbm;
   std::thread worker;
-  std::vector<std::thread> hbm_workers;  // run HBM-path requests concurrently
-  std::deque<void*> hbm_queue;           // admitted slots waiting for an HBM worker
+  std::vector<std::thread> hbm_workers;
+  std::deque<Member> hbm_queue;  // admitted HBM-path requests waiting for a worker
+  int hbm_running = 0;
   bool hbm_stop = false;
   bool stop = false;
   uint64_t next_ticket = 1;
@@ -658,6 +761,7 @@ struct mcrg_server {
     mcrg_request r;
     int nl;
     size_t bytes;
+    int threads;  // resident: threads per chain in the serve loop; 0: HBM path
     double submit_s;
   };
   std::deque<Req> pending;
@@ -668,6 +772,36 @@ struct mcrg_server {
   uint8_t* arena = nullptr;
   std::map<size_t, size_t> free_list;  // offset -> size
   int64_t budget = 0;
+  // the ring and its control block (page-locked, mapped), the claim counter (device)
+  int sms = 0;
+  uint32_t cap = 0;
+  ServeEntry* ring_h = nullptr;
+  ServeCtl* ctl_h = nullptr;
+  unsigned int* done_h = nullptr;
+  mcrg_moments* bins_h = nullptr;  // slots x kServeBinsPerChain
+  mcrg_moments* bins_d = nullptr;  // the same bins, device address
+  ServeArgs args{};
+  std::vector<int> free_bins;  // host bin slots not in use
+  std::vector<EntryState> entries;
+  uint64_t published = 0;
+  // launches of the loop, each on a stream of its own (a launch queued behind a
+  // running one on the same stream would not start until that one ended)
+  static constexpr int kMaxLoopStreams = 256;
+  struct LoopStream {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t end = nullptr;  // recorded after the stream's last launch
+    bool live = false;          // that launch may still run
+  };
+  std::vector<LoopStream> loop_streams;
+  int serve_grid = 0;                  // CTAs that fill the device
+  int64_t loop_launches = 0;
+  int64_t ctas_launched = 0;
+  // device counters (claimed, started, left) and their page-locked read-back
+  unsigned long long* h_ctr = nullptr;
+  unsigned long long seen[3] = {0, 0, 0};
+  cudaStream_t ctr_stream = nullptr;
+  cudaEvent_t ctr_done = nullptr;
+  bool ctr_pending = false;
 };
 
 namespace {
@@ -702,203 +836,310 @@ void arena_free(mcrg_server* s, size_t off, size_t bytes) {
   }
 }
 
-size_t request_bytes(const mcrg_request* r) {
-  // state + device bins + job descriptor
-  return (size_t)r->L * r->L + sizeof(mcrg_moments) * (size_t)(n_dev_bins(r) > 0 ? n_dev_bins(r) : 1) +
-         sizeof(ChainJob) + 3 * 256;
+// Whether a request runs in the serve loop: a resident chain whose bins fit
+// its host bin slot.
+int serve_threads(int device, const mcrg_request* r, int nl);
+
+// Device bytes a request holds while admitted: the final configuration of a
+// resident chain (its moments go to host bins), or every buffer of the
+// context an HBM-path request runs on.
+size_t request_bytes(const mcrg_request* r, int nl, bool resident) {
+  if (resident) return ((size_t)r->L * r->L + 255) & ~size_t(255);
+  return context_bytes(r->L, nl, r->n_couplings, r->flags, r->n_samples);
 }
 
-struct Slot {
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
-  bool busy = false;
-  uint64_t ticket = 0;
-  size_t off = 0, bytes = 0;
-  int nl = 0;
-  mcrg_request r{};
-  double submit_s = 0;
-  mcrg_moments* h_bins = nullptr;  // pinned
-  int64_t nb = 0;
-  bool tiled = false;
-};
+// Threads per chain of a shape in the serve loop.  A served request waits
+// for its own chain, so among the candidates the autotuner has timed for the
+// shape in this process the one with the lowest latency under load is taken,
+// as long as its throughput is within 20 % of the best; without timings the
+// fixed rule (the server does not time trials next to running requests).
+int serve_threads(int device, const mcrg_request* r, int nl) {
+  const int mode = chain_mode(r);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(std::make_tuple(device, r->L, mode, nl, r->n_couplings));
+  if (it == g_tune.end()) return resident_threads(r->L, r->flags != 0);
+  double best_rate = 0;
+  for (const Candidate& c : it->second.cand) best_rate = std::max(best_rate, c.rate);
+  int g = it->second.threads;
+  double lat = -1;
+  for (const Candidate& c : it->second.cand)
+    if (c.rate >= 0.8 * best_rate && c.s_sample > 0 && (lat < 0 || c.s_sample < lat)) {
+      lat = c.s_sample;
+      g = c.threads;
+    }
+  return g;
+}
 
-constexpr int kHbmWorkersDefault = 16;  // HBM-path requests are small, latency-bound launches: overlap many
-constexpr int kHbmWorkersMax = 256;
+// Threads per chain when the request runs in the serve loop, 0 when it runs
+// on the HBM path (no resident chain holds it, its bins exceed the host bin
+// slot, or no pack of the loop's CTA fits it).
+int serve_plan(const mcrg_request* r, int nl, int device) {
+  if (!runs_resident(r, nl) || n_dev_bins(r) > kServeBinsPerChain) return 0;
+  const int g = serve_threads(device, r, nl);
+  int per = 0, stride = 0;
+  return pack_geometry(r->L, nl, r->n_couplings, chain_mode(r), g, kServeThreads, &per, &stride) ? g : 0;
+}
 
-// One HBM-path worker: takes admitted slots from the queue and runs them on
-// contexts it keeps per (L, levels, couplings), re-initialised per request so
-// that no request pays a device allocation (which can synchronise the device
-// and stall the other slots).
+void finish(mcrg_server* s, const Member& m, const mcrg_result& res) {
+  s->done[m.ticket] = res;
+  s->submitted.erase(m.ticket);
+  arena_free(s, m.off, m.bytes);
+  s->bytes_in_use -= (int64_t)m.bytes;
+  s->in_flight--;
+  s->completed++;
+}
+
+// One HBM-path worker: runs admitted requests on contexts built in their
+// arena reservations (no cudaMalloc), one request at a time.
 void hbm_worker(mcrg_server* s) {
   cudaSetDevice(s->cfg.device);
-  std::map<std::tuple<int, int, int>, mcrg_ctx*> cache;
   for (;;) {
-    Slot* sl = nullptr;
+    Member m;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_hbm.wait(lk, [&] { return s->hbm_stop || !s->hbm_queue.empty(); });
       if (s->hbm_queue.empty()) break;  // stop requested and nothing left
-      sl = static_cast<Slot*>(s->hbm_queue.front());
+      m = s->hbm_queue.front();
       s->hbm_queue.pop_front();
+      s->hbm_running++;
     }
     mcrg_result res;
     memset(&res, 0, sizeof res);
-    res.submit_s = sl->submit_s;
-    const mcrg_request& r = sl->r;
-    if (r.L > MCRG_SMEM_MAX_L && make_accept(r.K).fast) {
-      const auto key = std::make_tuple(r.L, sl->nl, r.n_couplings);
-      mcrg_ctx* c = nullptr;
-      int rc = MCRG_OK;
-      auto it = cache.find(key);
-      if (it != cache.end()) {
-        c = it->second;
-        rc = reinit_context(c, r.K, r.seed, r.replica);
-      } else {
-        mcrg_cfg cfg;
-        memset(&cfg, 0, sizeof cfg);
-        cfg.L = r.L;
-        cfg.b = 2;
-        cfg.n_levels = sl->nl;
-        cfg.n_couplings = r.n_couplings;
-        cfg.K = r.K;
-        cfg.seed = r.seed;
-        cfg.replica = r.replica;
-        cfg.device = s->cfg.device;
-        rc = mcrg_alloc(&c, &cfg);
-        if (!rc) cache[key] = c;
-      }
+    res.submit_s = m.submit_s;
+    const mcrg_request& r = m.r;
+    DevSpan span;
+    span.base = s->arena + m.off;
+    span.cap = m.bytes;
+    mcrg_cfg cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.L = r.L;
+    cfg.b = 2;
+    cfg.n_levels = m.nl;
+    cfg.n_couplings = r.n_couplings;
+    cfg.K = r.K;
+    cfg.seed = r.seed;
+    cfg.replica = r.replica;
+    cfg.device = s->cfg.device;
+    mcrg_ctx* c = nullptr;
+    int rc = context_create(&c, &cfg, &span);
+    if (!rc) {
       if (r.flags) {
-        if (!rc) rc = mcrg_cluster_update(c, r.n_eq, r.flags, nullptr);
+        rc = mcrg_cluster_update(c, r.n_eq, r.flags, nullptr);
         if (!rc) rc = mcrg_measure_cluster(c, r.n_samples, r.sweeps_between, r.flags, &res.moments, 0, nullptr, 0);
       } else {
-        if (!rc) rc = mcrg_sweep(c, r.n_eq);
+        rc = mcrg_sweep(c, r.n_eq);
         if (!rc) rc = mcrg_measure(c, r.n_samples, r.sweeps_between, &res.moments, 0, nullptr, 0);
       }
-      res.status = rc;
-    } else {  // outside the fast acceptance regime: a one-off context
-      res.status = run_tiled_request(&r, s->cfg.device, &res.moments);
     }
+    if (c) mcrg_free(c);
+    res.status = rc;
     res.done_s = mono_s();
     std::lock_guard<std::mutex> lk(s->mu);
-    s->done[sl->ticket] = res;
-    s->submitted.erase(sl->ticket);
-    arena_free(s, sl->off, sl->bytes);
-    s->bytes_in_use -= (int64_t)sl->bytes;
-    s->in_flight--;
-    s->completed++;
-    sl->busy = false;
+    s->hbm_running--;
+    finish(s, m, res);
     s->cv_done.notify_all();
     s->cv_work.notify_all();
   }
-  for (auto& kv : cache) mcrg_free(kv.second);
+}
+
+// Keeps the serve loop at its width: reads the device counters back (one
+// small asynchronous copy in flight at a time) and, while published entries
+// are unclaimed and fewer CTAs than the target are running or queued,
+// launches the difference on the next stream of the pool.  Returns MCRG_EIO
+// when a launch of the loop has failed.
+int ensure_loop(mcrg_server* s, bool hbm_waiting) {
+  int live = 0;
+  mcrg_server::LoopStream* idle = nullptr;
+  for (auto& ls : s->loop_streams) {  // reap finished launches
+    if (ls.live) {
+      const cudaError_t q = cudaEventQuery(ls.end);
+      if (q == cudaSuccess) ls.live = false;
+      else if (q != cudaErrorNotReady) return MCRG_EIO;
+    }
+    if (ls.live) ++live;
+    else if (!idle) idle = &ls;
+  }
+  if (s->ctr_pending && cudaEventQuery(s->ctr_done) == cudaSuccess) {
+    for (int k = 0; k < 3; ++k) s->seen[k] = std::max(s->seen[k], s->h_ctr[k]);
+    s->ctr_pending = false;
+  }
+  if (!s->ctr_pending && live) {
+    if (cudaMemcpyAsync(s->h_ctr, s->args.ctr, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                        s->ctr_stream) == cudaSuccess &&
+        cudaEventRecord(s->ctr_done, s->ctr_stream) == cudaSuccess)
+      s->ctr_pending = true;
+  }
+  // HBM-path kernels need SMs the loop would hold: the loop leaves room for them while they wait
+  const int target = hbm_waiting ? std::max(1, s->serve_grid - std::max(2, s->sms / 8)) : s->serve_grid;
+  __atomic_store_n(&s->ctl_h->max_live, target, __ATOMIC_RELAXED);
+  if (!live) {  // nothing runs: every launched CTA has left
+    for (int k = 1; k < 3; ++k) s->seen[k] = (unsigned long long)s->ctas_launched;
+  }
+  bool waiting = false;
+  for (size_t k = 0; k < s->entries.size() && !waiting; ++k)
+    waiting = s->entries[k].busy && __atomic_load_n(&s->done_h[k], __ATOMIC_ACQUIRE) != (unsigned)s->entries[k].seq;
+  if (!waiting || s->published <= s->seen[0]) return MCRG_OK;  // nothing unclaimed
+  const int64_t running = s->ctas_launched - (int64_t)s->seen[2];
+  if (running >= target) return MCRG_OK;
+  if (!idle) {  // every stream holds a running launch: one more, up to the cap
+    if ((int)s->loop_streams.size() >= mcrg_server::kMaxLoopStreams) return MCRG_OK;
+    mcrg_server::LoopStream ls;
+    if (cudaStreamCreateWithFlags(&ls.stream, cudaStreamNonBlocking) != cudaSuccess) return MCRG_EIO;
+    if (cudaEventCreateWithFlags(&ls.end, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(ls.stream);
+      return MCRG_EIO;
+    }
+    s->loop_streams.push_back(ls);
+    idle = &s->loop_streams.back();
+  }
+  const int grid = (int)(target - running);
+  ServeArgs a = s->args;
+  void* argv[] = {&a};
+  if (cudaLaunchKernel(serve_kernel_fn(), dim3(grid), dim3(kServeThreads), argv, (size_t)kPoolMaxSmem,
+                       idle->stream) != cudaSuccess ||
+      cudaEventRecord(idle->end, idle->stream) != cudaSuccess)
+    return MCRG_EIO;
+  idle->live = true;
+  s->ctas_launched += grid;
+  __atomic_add_fetch(&s->loop_launches, 1, __ATOMIC_RELAXED);
+  return MCRG_OK;
 }
 
 void server_loop(mcrg_server* s) {
   cudaSetDevice(s->cfg.device);
-  std::vector<Slot> slots((size_t)s->cfg.slots);
-  for (auto& sl : slots) {
-    cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
-    cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-  }
   for (;;) {
-    // ---- admit
-    std::vector<std::pair<Slot*, mcrg_server::Req>> launch;
+    bool progressed = false;
+    // ---- admit: pending requests in arrival order while slots, bins and memory allow
+    std::vector<std::vector<Member>> packs;
+    std::vector<PoolPack> shapes;  // per pack: threads, stride (count filled at publish)
+    bool hbm_waiting = false;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      bool any_busy = false;
-      for (auto& sl : slots) any_busy |= sl.busy;
-      if (!any_busy && s->pending.empty()) {
+      const bool idle = s->pending.empty() && s->in_flight == 0;
+      if (idle) {
         if (s->stop) break;
         s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
         continue;
       }
-      for (auto& sl : slots) {
-        if (sl.busy || s->pending.empty()) continue;
+      std::map<std::tuple<int, int, int, int, int>, size_t> open;  // shape -> pack index still filling
+      size_t free_entries = 0;  // ring slots free in publication order from the next one on
+      while (free_entries < s->cap && !s->entries[(size_t)((s->published + free_entries) % s->cap)].busy)
+        ++free_entries;
+      while (!s->pending.empty()) {
         mcrg_server::Req& q = s->pending.front();
+        const bool resident = q.threads > 0;
+        if (resident && s->free_bins.empty()) break;
+        const auto key = std::make_tuple(q.r.L, chain_mode(&q.r), q.nl, q.r.n_couplings, q.threads);
+        auto it = resident ? open.find(key) : open.end();
+        if (resident && it == open.end() && packs.size() >= free_entries) break;  // no ring slot
         size_t off = (size_t)-1;
         if ((int64_t)q.bytes + s->bytes_in_use <= s->budget) off = arena_alloc(s, q.bytes);
         if (off == (size_t)-1) break;  // wait for memory (keeps arrival order)
-        sl.busy = true;
-        sl.off = off;
-        sl.bytes = q.bytes;
+        Member m{q.ticket, q.r, q.nl, q.submit_s, off, q.bytes, -1};
         s->bytes_in_use += (int64_t)q.bytes;
         s->admitted++;
         s->in_flight++;
-        launch.push_back({&sl, q});
-        s->pending.pop_front();
-      }
-    }
-    for (auto& lp : launch) {
-      Slot& sl = *lp.first;
-      const mcrg_server::Req& q = lp.second;
-      sl.ticket = q.ticket;
-      sl.r = q.r;
-      sl.nl = q.nl;
-      sl.submit_s = q.submit_s;
-      sl.nb = n_dev_bins(&q.r);
-      sl.tiled = !runs_resident(&q.r, q.nl);
-      if (sl.tiled) continue;  // handed to the HBM workers below
-      uint8_t* base = s->arena + sl.off;
-      ChainJob* d_job = reinterpret_cast<ChainJob*>(base);
-      mcrg_moments* d_bins = reinterpret_cast<mcrg_moments*>(base + 256);
-      uint8_t* d_state = base + 256 + ((sizeof(mcrg_moments) * (size_t)(sl.nb > 0 ? sl.nb : 1) + 255) & ~size_t(255));
-      ChainJob j;
-      fill_job(&j, &q.r, q.nl, d_state, d_bins);
-      if (!sl.h_bins) cudaMallocHost(&sl.h_bins, sizeof(mcrg_moments) * 4);
-      if (sl.nb > 4) {
-        cudaFreeHost(sl.h_bins);
-        cudaMallocHost(&sl.h_bins, sizeof(mcrg_moments) * (size_t)sl.nb);
-      }
-      cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, sl.stream);
-      cudaMemsetAsync(d_bins, 0, sizeof(mcrg_moments) * (size_t)(sl.nb > 0 ? sl.nb : 1), sl.stream);
-      launch_chain(d_job, 1, j.L, j.n_levels, j.C, j.threads, j.acc.fast && j.L >= 64, sl.stream, j.update != 0);
-      if (sl.nb > 0)
-        cudaMemcpyAsync(sl.h_bins, d_bins, sizeof(mcrg_moments) * (size_t)sl.nb, cudaMemcpyDeviceToHost, sl.stream);
-      cudaEventRecord(sl.done, sl.stream);
-    }
-    // ---- hand HBM-path admissions to the worker pool (they run concurrently, each on its own stream)
-    {
-      bool any = false;
-      std::lock_guard<std::mutex> lk(s->mu);
-      for (auto& lp : launch)
-        if (lp.first->tiled) {
-          s->hbm_queue.push_back(lp.first);
-          any = true;
+        if (resident) {
+          m.bin_slot = s->free_bins.back();
+          s->free_bins.pop_back();
+          if (it == open.end()) {
+            const int g = q.threads;
+            int per = 0, stride = 0;
+            pack_geometry(q.r.L, q.nl, q.r.n_couplings, chain_mode(&q.r), g, kServeThreads, &per, &stride);
+            packs.emplace_back();
+            shapes.push_back(PoolPack{0, (int16_t)std::max(per, 1), (int16_t)g, stride, 0});
+            it = open.emplace(key, packs.size() - 1).first;
+          }
+          packs[it->second].push_back(m);
+          if ((int)packs[it->second].size() >= shapes[it->second].count) open.erase(it);
+        } else {
+          s->hbm_queue.push_back(m);
+          s->cv_hbm.notify_one();
         }
-      if (any) s->cv_hbm.notify_all();
+        s->pending.pop_front();
+        progressed = true;
+      }
+      hbm_waiting = !s->hbm_queue.empty() || s->hbm_running > 0;
     }
-    // ---- retire finished slots
-    bool progressed = false;
-    for (auto& sl : slots) {
-      if (sl.tiled || !sl.busy) continue;  // HBM-path slots are retired by their worker
-      const cudaError_t q = cudaEventQuery(sl.done);
-      if (q == cudaErrorNotReady) continue;
-      mcrg_result res;
-      memset(&res, 0, sizeof res);
-      res.submit_s = sl.submit_s;
-      res.status = q == cudaSuccess ? MCRG_OK : MCRG_EIO;
-      res.moments.n_levels = sl.nl;
-      res.moments.n_couplings = sl.r.n_couplings;
-      for (int64_t b = 0; b < sl.nb; ++b) add_into(&res.moments, &sl.h_bins[b]);
-      res.done_s = mono_s();
+    // ---- publish: entry contents first, then the tail (release)
+    for (size_t p = 0; p < packs.size(); ++p) {
+      const uint32_t slot = (uint32_t)(s->published % s->cap);  // free: admission counted it
+      EntryState& es = s->entries[slot];
+      ServeEntry& e = s->ring_h[slot];
+      PoolPack pk = shapes[p];
+      pk.count = (int16_t)packs[p].size();
+      e.pk = pk;
+      for (size_t k = 0; k < packs[p].size(); ++k) {
+        const Member& m = packs[p][k];
+        memset(s->bins_h + (size_t)m.bin_slot * kServeBinsPerChain, 0, sizeof(mcrg_moments) * kServeBinsPerChain);
+        fill_job(&e.jobs[k], &m.r, m.nl, s->arena + m.off, s->bins_d + (size_t)m.bin_slot * kServeBinsPerChain);
+        e.jobs[k].threads = pk.threads;
+      }
+      es.busy = true;
+      es.seq = s->published + 1;
+      es.members = packs[p];
+      __atomic_store_n(&s->ctl_h->tail, (unsigned long long)(s->published + 1), __ATOMIC_RELEASE);
+      __atomic_add_fetch(&s->published, 1, __ATOMIC_RELAXED);
+      progressed = true;
+    }
+    // ---- keep the loop running while entries wait
+    if (ensure_loop(s, hbm_waiting) != MCRG_OK) {  // the loop failed: every entry it held fails
       std::lock_guard<std::mutex> lk(s->mu);
-      s->done[sl.ticket] = res;
-      s->submitted.erase(sl.ticket);
-      arena_free(s, sl.off, sl.bytes);
-      s->bytes_in_use -= (int64_t)sl.bytes;
-      s->in_flight--;
-      s->completed++;
-      sl.busy = false;
+      for (auto& e : s->entries)
+        if (e.busy) {
+          for (auto& m : e.members) {
+            mcrg_result res;
+            memset(&res, 0, sizeof res);
+            res.status = MCRG_EIO;
+            res.submit_s = m.submit_s;
+            res.done_s = mono_s();
+            s->free_bins.push_back(m.bin_slot);
+            finish(s, m, res);
+          }
+          e.busy = false;
+          e.members.clear();
+        }
+      s->cv_done.notify_all();
+    }
+    // ---- retire finished entries
+    for (uint32_t k = 0; k < s->cap; ++k) {
+      EntryState& e = s->entries[k];
+      if (!e.busy) continue;
+      const unsigned int d = __atomic_load_n(&s->done_h[k], __ATOMIC_ACQUIRE);
+      if (d != (unsigned int)e.seq) continue;
+      const double t_done = mono_s();
+      std::vector<mcrg_result> res(e.members.size());
+      for (size_t q = 0; q < e.members.size(); ++q) {
+        const Member& m = e.members[q];
+        mcrg_result& r = res[q];
+        memset(&r, 0, sizeof r);
+        r.submit_s = m.submit_s;
+        r.done_s = t_done;
+        r.status = MCRG_OK;
+        r.moments.n_levels = m.nl;
+        r.moments.n_couplings = m.r.n_couplings;
+        const mcrg_moments* hb = s->bins_h + (size_t)m.bin_slot * kServeBinsPerChain;
+        for (int64_t b = 0; b < n_dev_bins(&m.r); ++b) add_into(&r.moments, &hb[b]);
+        r.moments.n_levels = m.nl;
+        r.moments.n_couplings = m.r.n_couplings;
+      }
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (size_t q = 0; q < e.members.size(); ++q) {
+        s->free_bins.push_back(e.members[q].bin_slot);
+        finish(s, e.members[q], res[q]);
+      }
+      e.busy = false;
+      e.members.clear();
       progressed = true;
       s->cv_done.notify_all();
     }
-    if (!progressed && launch.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
-  for (auto& sl : slots) {
-    cudaStreamSynchronize(sl.stream);
-    cudaStreamDestroy(sl.stream);
-    cudaEventDestroy(sl.done);
-    if (sl.h_bins) cudaFreeHost(sl.h_bins);
+  // stop: every admitted request has finished; the loop's CTAs leave
+  __atomic_store_n(&s->ctl_h->stop, 1, __ATOMIC_RELEASE);
+  for (auto& ls : s->loop_streams) {
+    cudaStreamSynchronize(ls.stream);
+    ls.live = false;
   }
 }
 
@@ -916,11 +1157,61 @@ int mcrg_server_create(mcrg_server** out, const mcrg_server_cfg* cfg) {
   if (!s) return MCRG_ENOMEM;
   s->cfg = *cfg;
   s->budget = cfg->hbm_budget_bytes;
-  if (cudaMalloc(&s->arena, (size_t)s->budget) != cudaSuccess) {
+  int rc = MCRG_OK;
+  do {
+    if (cudaMalloc(&s->arena, (size_t)s->budget) != cudaSuccess) { rc = MCRG_ENOMEM; break; }
+    s->free_list[0] = (size_t)s->budget & ~size_t(255);
+    int occ = 0;
+    if (cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, cfg->device) != cudaSuccess ||
+        serve_prepare(kPoolMaxSmem, &occ) != cudaSuccess || occ < 1) {
+      rc = MCRG_EIO;
+      break;
+    }
+    s->serve_grid = s->sms * occ;
+    s->cap = (uint32_t)(4 * cfg->slots);
+    if (cudaHostAlloc(&s->ring_h, sizeof(ServeEntry) * s->cap, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostAlloc(&s->ctl_h, sizeof(ServeCtl), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostAlloc(&s->done_h, sizeof(unsigned int) * s->cap, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostAlloc(&s->bins_h, sizeof(mcrg_moments) * kServeBinsPerChain * (size_t)cfg->slots,
+                      cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostAlloc(&s->h_ctr, 4 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess ||
+        cudaMalloc(&s->args.ctr, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+      rc = MCRG_ENOMEM;
+      break;
+    }
+    memset(s->ring_h, 0, sizeof(ServeEntry) * s->cap);
+    memset(s->ctl_h, 0, sizeof(ServeCtl));
+    memset(s->done_h, 0, sizeof(unsigned int) * s->cap);
+    s->ctl_h->idle_ns = kServeIdleNs;
+    if (cudaHostGetDevicePointer((void**)&s->args.ring, s->ring_h, 0) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&s->args.ctl, s->ctl_h, 0) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&s->args.done, s->done_h, 0) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&s->bins_d, s->bins_h, 0) != cudaSuccess ||
+        cudaMemset(s->args.ctr, 0, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->ctr_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ctr_done, cudaEventDisableTiming) != cudaSuccess) {
+      rc = MCRG_EIO;
+      break;
+    }
+    memset(s->h_ctr, 0, 4 * sizeof(unsigned long long));
+    s->ctl_h->max_live = s->serve_grid;
+    s->args.cap = s->cap;
+    s->entries.resize(s->cap);
+    for (int b = cfg->slots - 1; b >= 0; --b) s->free_bins.push_back(b);
+  } while (0);
+  if (rc) {
+    cudaFree(s->arena);
+    cudaFree(s->args.ctr);
+    if (s->ring_h) cudaFreeHost(s->ring_h);
+    if (s->ctl_h) cudaFreeHost(s->ctl_h);
+    if (s->done_h) cudaFreeHost(s->done_h);
+    if (s->bins_h) cudaFreeHost(s->bins_h);
+    if (s->h_ctr) cudaFreeHost(s->h_ctr);
+    if (s->ctr_stream) cudaStreamDestroy(s->ctr_stream);
+    if (s->ctr_done) cudaEventDestroy(s->ctr_done);
     delete s;
-    return MCRG_ENOMEM;
+    return rc;
   }
-  s->free_list[0] = (size_t)s->budget & ~size_t(255);
   s->worker = std::thread(server_loop, s);
   const int nw = cfg->hbm_workers > 0 ? cfg->hbm_workers : kHbmWorkersDefault;
   for (int w = 0; w < nw; ++w) s->hbm_workers.emplace_back(hbm_worker, s);
@@ -932,12 +1223,13 @@ int mcrg_submit(mcrg_server* s, const mcrg_request* r, uint64_t* ticket) {
   if (!s || !r || !ticket) return MCRG_EINVAL;
   const int nl = check_request(r);
   if (nl < 0) return nl;
-  const size_t bytes = request_bytes(r);
+  const int threads = serve_plan(r, nl, s->cfg.device);
+  const size_t bytes = request_bytes(r, nl, threads > 0);
   if ((int64_t)bytes > s->budget) return MCRG_ENOSPC;
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->stop) return MCRG_ECANCELED;
   if ((int)s->pending.size() >= s->cfg.queue_capacity) return MCRG_EBUSY;
-  mcrg_server::Req q{s->next_ticket++, *r, nl, bytes, mono_s()};
+  mcrg_server::Req q{s->next_ticket++, *r, nl, bytes, threads, mono_s()};
   s->pending.push_back(q);
   s->submitted[q.ticket] = q.submit_s;
   *ticket = q.ticket;
@@ -1013,6 +1305,14 @@ int mcrg_server_stats(mcrg_server* s, int64_t* admitted, int64_t* completed, int
   return MCRG_OK;
 }
 
+int mcrg_server_loop_stats(mcrg_server* s, int64_t* loop_launches, int64_t* entries_published) {
+  if (!s) return MCRG_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);  // the scheduler thread updates both under its own order; a snapshot
+  if (loop_launches) *loop_launches = __atomic_load_n(&s->loop_launches, __ATOMIC_RELAXED);
+  if (entries_published) *entries_published = (int64_t)__atomic_load_n(&s->published, __ATOMIC_RELAXED);
+  return MCRG_OK;
+}
+
 int mcrg_server_destroy(mcrg_server* s) {
   if (!s) return MCRG_EINVAL;
   {
@@ -1040,7 +1340,21 @@ int mcrg_server_destroy(mcrg_server* s) {
   for (auto& t : s->hbm_workers)
     if (t.joinable()) t.join();
   cudaSetDevice(s->cfg.device);
+  for (auto& ls : s->loop_streams) {
+    cudaStreamSynchronize(ls.stream);
+    cudaStreamDestroy(ls.stream);
+    cudaEventDestroy(ls.end);
+  }
+  cudaStreamSynchronize(s->ctr_stream);
+  cudaStreamDestroy(s->ctr_stream);
+  cudaEventDestroy(s->ctr_done);
   cudaFree(s->arena);
+  cudaFree(s->args.ctr);
+  cudaFreeHost(s->ring_h);
+  cudaFreeHost(s->ctl_h);
+  cudaFreeHost(s->done_h);
+  cudaFreeHost(s->bins_h);
+  cudaFreeHost(s->h_ctr);
   delete s;
   return MCRG_OK;
 }

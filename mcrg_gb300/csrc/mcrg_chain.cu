@@ -264,6 +264,8 @@ __global__ void __launch_bounds__(kServeThreads, 1) serve_kernel(ServeArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ long long s_idx;
   __shared__ __align__(16) ServeEntry s_entry;
+  volatile unsigned long long* vctr = a.ctr;
+  if (threadIdx.x == 0) atomicAdd(a.ctr + 1, 1ull);
   for (;;) {
     if (threadIdx.x == 0) {
       long long got = -1;
@@ -272,11 +274,11 @@ __global__ void __launch_bounds__(kServeThreads, 1) serve_kernel(ServeArgs a) {
       unsigned ns = 128;
       for (;;) {
         if (ld_volatile_s32(&a.ctl->stop)) break;
-        if ((int)blockIdx.x >= (int)gridDim.x - ld_volatile_s32(&a.ctl->shrink)) break;
+        if ((long long)(vctr[1] - vctr[2]) > (long long)ld_volatile_s32(&a.ctl->max_live)) break;
         const unsigned long long tail = ld_acquire_sys(&a.ctl->tail);
-        const unsigned long long h = *reinterpret_cast<volatile unsigned long long*>(a.head);
+        const unsigned long long h = vctr[0];
         if (h < tail) {
-          if (atomicCAS(a.head, h, h + 1) == h) {
+          if (atomicCAS(a.ctr, h, h + 1) == h) {
             got = (long long)h;
             break;
           }
@@ -287,6 +289,7 @@ __global__ void __launch_bounds__(kServeThreads, 1) serve_kernel(ServeArgs a) {
         if (ns < 4096) ns <<= 1;
       }
       s_idx = got;
+      if (got < 0) atomicAdd(a.ctr + 2, 1ull);  // this CTA leaves
     }
     __syncthreads();
     const long long idx = s_idx;

@@ -159,23 +159,27 @@ struct PoolQueue {
 // acquire load of `tail`, runs its chains (the moments go to the jobs' bins,
 // page-locked host memory) and stores done[k % cap] = k + 1 with release
 // semantics.  A CTA with nothing to claim polls with growing sleeps and
-// leaves after `idle_ns`; the CTAs with blockIdx.x >= gridDim.x - shrink
-// leave at their next claim (space for HBM-path kernels); all leave at stop.
-struct ServeEntry {
+// leaves after `idle_ns`; a CTA also leaves at its next claim while more than
+// `max_live` CTAs run (room for HBM-path kernels), and all leave at stop.
+// The device counters ctr[0..2] = entries claimed, CTAs started, CTAs left
+// (monotonic) let the server keep the loop at its width: it launches more
+// CTAs, on a pool of streams, while entries wait and fewer are running.
+struct __align__(16) ServeEntry {
   PoolPack pk;  // pk.first unused: the jobs are inline
   ChainJob jobs[kPoolMaxGroups];
 };
+static_assert(sizeof(PoolPack) == 16 && sizeof(ServeEntry) % 16 == 0, "ring entries are copied as 16-byte words");
 struct ServeCtl {
   unsigned long long tail;
   unsigned long long idle_ns;
   int32_t stop;
-  int32_t shrink;
+  int32_t max_live;
 };
 struct ServeArgs {
   const ServeEntry* ring;   // device address of the host ring
   ServeCtl* ctl;            // device address of the host control block
   unsigned int* done;       // device address of the host completion words
-  unsigned long long* head; // device memory: entries claimed so far
+  unsigned long long* ctr;  // device memory: [0] entries claimed, [1] CTAs started, [2] CTAs left
   uint32_t cap;
   uint32_t pad;
 };

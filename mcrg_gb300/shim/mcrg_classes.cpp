@@ -70,12 +70,19 @@ void Lattice::sync_spins() {
     for (int j = 0; j < N_; ++j) spins_(i, j) = h[(size_t)i * N_ + j];
 }
 
-std::vector<double> Lattice::calc_interactions() {
+Interactions Lattice::calc_interactions() {
   const int nl = (int)std::lround(std::log2((double)N_)) - 1;
   std::vector<int64_t> S((size_t)(nl + 1) * 2 + 8, 0);
   // level 0 only is returned, as the reference's calc_interactions does
   check(mcrg_interactions(ctx_, S.data()), "mcrg_interactions");
+#ifdef MCRG_EIGEN_SPINS
+  Interactions r;
+  r(0) = (double)S[0];
+  r(1) = (double)S[1];
+  return r;
+#else
   return {(double)S[0], (double)S[1]};
+#endif
 }
 
 double Lattice::calc_nearest_neighbor_interaction() { return calc_interactions()[0]; }
@@ -123,7 +130,7 @@ IsingModel::IsingModel(double K) : K_(K), P_(1.0 - std::exp(2.0 * K)) {}
 namespace {
 
 // the reference's write_iter (src/definitions.cpp:44-68): logged iterations
-bool write_iter(int i) {
+bool logged_iteration(int i) {
   if (i < 10) return true;
   if (i < 100) return i % 10 == 0;
   if (i < 1000) return i % 100 == 0;
@@ -175,7 +182,7 @@ void IsingModel::equilibrate(std::shared_ptr<Lattice> p, int n_samples_eq, bool 
   int done = 0;
   try {
     for (int n = 1; n <= n_samples_eq; ++n) {
-      if (!write_iter(n)) continue;
+      if (!logged_iteration(n)) continue;
       check(advance(p->ctx(), update_, n - done), "equilibrate");
       done = n;
       p->sync_spins();

@@ -39,6 +39,15 @@ class McrgError : public std::runtime_error {
   int code_;
 };
 
+#ifdef MCRG_EIGEN_SPINS
+// The drop-in build (headers in dropin/, compiled with the reference's own
+// definitions.hpp and vendored Eigen): spins_ and the neighbour tables are the
+// reference's `imat`, calc_interactions returns its `vec2D`, so callers that
+// hand spins_ to Eigen code (src/rgnn.cpp:113-114,175) compile unchanged.
+#include "definitions.hpp"
+using SpinMatrix = imat;
+using Interactions = vec2D;
+#else
 // Minimal stand-in for the reference's `imat` (Eigen column-major int
 // matrix): spins_(i, j) indexing, rows(), cols(), sum().
 class SpinMatrix {
@@ -59,6 +68,8 @@ class SpinMatrix {
   int n_ = 0, m_ = 0;
   std::vector<int> d_;
 };
+using Interactions = std::vector<double>;
+#endif
 
 class Lattice {
  public:
@@ -76,7 +87,8 @@ class Lattice {
   bool mirror_spins_ = true;
 
   // src/lattice.cpp:102-120 -> (S_nn, S_nnn) of the current configuration
-  std::vector<double> calc_interactions();
+  // (every coupling of the context in the stand-alone build)
+  Interactions calc_interactions();
   double calc_nearest_neighbor_interaction();
 
   // src/lattice.cpp:63-75: "\n" then one "# s, s, ..., " line per row of the

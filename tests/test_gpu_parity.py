@@ -290,10 +290,10 @@ def test_server_alone_and_in_the_mix(M):
 
 def test_server_hbm_requests_in_the_mix(M):
     """Requests too large for a resident chain (L = 2048) or outside the fast acceptance
-    regime (K = -0.1, L = 64) run on the server's worker pool, several with the same L so
-    that cached contexts are re-initialised between requests; L = 512 / 1024 in the fast
-    regime run as resident plane chains.  Every result equals the single-context run of the
-    same request, alone and while the others run."""
+    regime (K = -0.1, L = 64) run on the server's worker pool, on contexts built in their
+    reservations of the server's arena; L = 512 / 1024 in the fast regime run as resident
+    plane chains in the device-resident loop.  Every result equals the single-context run
+    of the same request, alone and while the others run."""
     rng = np.random.default_rng(5)
     reqs = []
     for i in range(14):
@@ -310,7 +310,7 @@ def test_server_hbm_requests_in_the_mix(M):
         for r, o in zip(reqs, out):
             assert o.status == 0, (r.L, o.status)
             assert_moments_equal(M.moments_from_c(o.moments), solo(M, r))
-        again = srv.wait(srv.submit(reqs[0]), 300)  # a reused context gives the same chain again
+        again = srv.wait(srv.submit(reqs[0]), 300)  # the same request again gives the same chain
         assert_moments_equal(M.moments_from_c(again.moments), M.moments_from_c(out[0].moments))
         st = srv.stats()
         assert st["completed"] == len(reqs) + 1 and st["in_flight"] == 0 and st["bytes_in_use"] == 0
