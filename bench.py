@@ -326,16 +326,19 @@ def plain_by_side(M, reqs, results, device, per_side: int, weights=None) -> dict
     """The plain one-lattice-per-launch path on `per_side` requests of every side
     in the mix (the same requests, seeds included).  Its solves/s on the whole mix
     is 1 / (expected seconds per request), the per-side means weighted by the
-    side's share of the mix (or `weights`).  Each plain result is compared with
-    the batched / served result of the same request (same seed: the same chain)."""
+    side's share of the mix (or `weights`).  A request's plain time grows with its
+    sample count, so the requests timed for a side are those whose sample counts
+    are closest to the mix's mean.  Each plain result is compared with the batched
+    / served result of the same request (same seed: the same chain)."""
     import numpy as np
     by = {}
     for i, r in enumerate(reqs):
         by.setdefault(int(r.L), []).append(i)
+    mean_n = float(np.mean([r.n_samples for r in reqs]))
     secs, identical, n = {}, True, 0
     for L in sorted(by):
         ts = []
-        for i in by[L][:per_side]:
+        for i in sorted(by[L], key=lambda i: abs(reqs[i].n_samples - mean_n))[:per_side]:
             dt, tot = time_plain(M, reqs[i], device)
             ts.append(dt)
             n += 1
@@ -634,6 +637,10 @@ class RefCPU:
         for t in ths:
             t.join()
 
+    def warm(self) -> None:
+        """One Wolff step on every replica (no measurement)."""
+        self._run(lambda k: self.wolff[k].steps(self.spins[k], 1))
+
     def step(self, seconds: float) -> dict:
         res = [None] * self.threads
 
@@ -742,7 +749,7 @@ def reference_arm(args):
     vals = []
     try:
         for _ in range(args.warmup):
-            ref.step(0.0)  # one sample per thread (at least), untimed
+            ref.warm()  # one Wolff step per replica, untimed
         for _ in range(args.steps):
             vals.append(ref.step(0.0))
     finally:
@@ -791,7 +798,7 @@ def main():
     ap.add_argument("--cluster-equilibrate", type=int, default=60, help="cluster workload: SW updates first")
     ap.add_argument("--plain-per-side", type=int, default=2, help="plain-path requests timed per lattice side")
     ap.add_argument("--plain-sweeps", type=int, default=10000)
-    ap.add_argument("--served-requests", type=int, default=800)
+    ap.add_argument("--served-requests", type=int, default=2000)
     ap.add_argument("--served-scale", type=float, default=1.0, help="sweeps of the served mix x this (1: as stated)")
     ap.add_argument("--served-slots", type=int, default=1024)
     ap.add_argument("--served-budget-gb", type=float, default=150.0)

@@ -727,6 +727,7 @@ constexpr int kServeBinsPerChain = 4;        // host bins per resident chain (2^
 constexpr int kHbmWorkersDefault = 16;
 constexpr int kHbmWorkersMax = 256;
 constexpr unsigned long long kServeIdleNs = 20000000ull;  // a CTA leaves after 20 ms without work
+constexpr double kServeHoldS = 1e-3;  // longest wait of a pack that is not full while the loop has a backlog
 
 struct Member {  // one admitted request
   uint64_t ticket;
@@ -796,6 +797,7 @@ struct mcrg_server {
   int serve_grid = 0;                  // CTAs that fill the device
   int64_t loop_launches = 0;
   int64_t ctas_launched = 0;
+  int live_launches = 0;               // launches of the loop that may still run (last count)
   // device counters (claimed, started, left) and their page-locked read-back
   unsigned long long* h_ctr = nullptr;
   unsigned long long seen[3] = {0, 0, 0};
@@ -959,6 +961,7 @@ int ensure_loop(mcrg_server* s, bool hbm_waiting) {
     if (ls.live) ++live;
     else if (!idle) idle = &ls;
   }
+  s->live_launches = live;
   if (s->ctr_pending && cudaEventQuery(s->ctr_done) == cudaSuccess) {
     for (int k = 0; k < 3; ++k) s->seen[k] = std::max(s->seen[k], s->h_ctr[k]);
     s->ctr_pending = false;
@@ -1000,6 +1003,7 @@ int ensure_loop(mcrg_server* s, bool hbm_waiting) {
       cudaEventRecord(idle->end, idle->stream) != cudaSuccess)
     return MCRG_EIO;
   idle->live = true;
+  s->live_launches++;
   s->ctas_launched += grid;
   __atomic_add_fetch(&s->loop_launches, 1, __ATOMIC_RELAXED);
   return MCRG_OK;
@@ -1007,11 +1011,18 @@ int ensure_loop(mcrg_server* s, bool hbm_waiting) {
 
 void server_loop(mcrg_server* s) {
   cudaSetDevice(s->cfg.device);
+  // Packs still filling, kept across passes: while the loop already has
+  // entries nobody has claimed, a pack that is not full waits (up to
+  // kServeHoldS) for more requests of its shape -- it could not start sooner
+  // anyway -- so a saturated loop runs full packs instead of one small chain
+  // per CTA.
+  std::vector<std::vector<Member>> packs;
+  std::vector<PoolPack> shapes;  // per pack: threads, stride (count filled at publish)
+  std::vector<double> opened;    // when each pack was opened
+  std::map<std::tuple<int, int, int, int, int>, size_t> open;  // shape -> pack index still filling
   for (;;) {
     bool progressed = false;
     // ---- admit: pending requests in arrival order while slots, bins and memory allow
-    std::vector<std::vector<Member>> packs;
-    std::vector<PoolPack> shapes;  // per pack: threads, stride (count filled at publish)
     bool hbm_waiting = false;
     {
       std::unique_lock<std::mutex> lk(s->mu);
@@ -1021,7 +1032,6 @@ void server_loop(mcrg_server* s) {
         s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
         continue;
       }
-      std::map<std::tuple<int, int, int, int, int>, size_t> open;  // shape -> pack index still filling
       size_t free_entries = 0;  // ring slots free in publication order from the next one on
       while (free_entries < s->cap && !s->entries[(size_t)((s->published + free_entries) % s->cap)].busy)
         ++free_entries;
@@ -1048,10 +1058,11 @@ void server_loop(mcrg_server* s) {
             pack_geometry(q.r.L, q.nl, q.r.n_couplings, chain_mode(&q.r), g, kServeThreads, &per, &stride);
             packs.emplace_back();
             shapes.push_back(PoolPack{0, (int16_t)std::max(per, 1), (int16_t)g, stride, 0});
+            opened.push_back(mono_s());
             it = open.emplace(key, packs.size() - 1).first;
           }
           packs[it->second].push_back(m);
-          if ((int)packs[it->second].size() >= shapes[it->second].count) open.erase(it);
+          if ((int)packs[it->second].size() >= shapes[it->second].count) open.erase(it);  // full: published next
         } else {
           s->hbm_queue.push_back(m);
           s->cv_hbm.notify_one();
@@ -1061,8 +1072,17 @@ void server_loop(mcrg_server* s) {
       }
       hbm_waiting = !s->hbm_queue.empty() || s->hbm_running > 0;
     }
-    // ---- publish: entry contents first, then the tail (release)
+    // ---- publish full packs, and the others unless the loop has a backlog (entry contents first,
+    //      then the tail with release semantics)
+    const bool backlog = s->live_launches > 0 && s->published > s->seen[0];
+    const double now = mono_s();
+    std::vector<size_t> keep;
     for (size_t p = 0; p < packs.size(); ++p) {
+      const bool full = (int)packs[p].size() >= shapes[p].count;
+      if (!full && backlog && now - opened[p] < kServeHoldS) {
+        keep.push_back(p);
+        continue;
+      }
       const uint32_t slot = (uint32_t)(s->published % s->cap);  // free: admission counted it
       EntryState& es = s->entries[slot];
       ServeEntry& e = s->ring_h[slot];
@@ -1081,6 +1101,22 @@ void server_loop(mcrg_server* s) {
       __atomic_store_n(&s->ctl_h->tail, (unsigned long long)(s->published + 1), __ATOMIC_RELEASE);
       __atomic_add_fetch(&s->published, 1, __ATOMIC_RELAXED);
       progressed = true;
+    }
+    if (keep.size() != packs.size()) {  // drop the published packs, keep the ones still filling
+      std::vector<std::vector<Member>> kp;
+      std::vector<PoolPack> ks;
+      std::vector<double> ko;
+      open.clear();
+      for (size_t p : keep) {
+        const Member& m0 = packs[p][0];
+        open[std::make_tuple(m0.r.L, chain_mode(&m0.r), m0.nl, m0.r.n_couplings, (int)shapes[p].threads)] = kp.size();
+        kp.push_back(std::move(packs[p]));
+        ks.push_back(shapes[p]);
+        ko.push_back(opened[p]);
+      }
+      packs.swap(kp);
+      shapes.swap(ks);
+      opened.swap(ko);
     }
     // ---- keep the loop running while entries wait
     if (ensure_loop(s, hbm_waiting) != MCRG_OK) {  // the loop failed: every entry it held fails
