@@ -30,6 +30,62 @@ __global__ void tiled_init_kernel(uint8_t* lat, int L, Key key, uint32_t rep) {
   init_level0(lat, L, key, rep, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
+// Exact update of colour c of an HBM lattice (L >= 64) for any coupling: the
+// acceptance outside the fast regime, where m = 0 or 1 anti-aligned
+// neighbours can always flip and m >= 2 draws (or the reverse for K > 0).
+// In place: a colour reads only the other colour.  One thread takes four
+// consecutive sites of a colour row, which share the 32-site word's two
+// high-byte blocks (groups 2w, 2w+1) and one low-bits block (group k >> 2):
+// the same draws, site for site, as the resident exact path and the fast
+// sweeps (u32 = r8 << 24 | r24, flip iff always[m] or u32 < thr[m]).
+__global__ void __launch_bounds__(256) exact_colour_kernel(uint8_t* __restrict__ lat, int L, int c, uint32_t t,
+                                                           Key key, uint32_t rep, Accept a) {
+  const int half = L / 2;
+  uint8_t* Cc = lat + (size_t)c * L * half;
+  const uint8_t* Oc = lat + (size_t)(1 - c) * L * half;
+  const long long quads = (long long)L * half / 4;
+  for (long long qd = (long long)blockIdx.x * blockDim.x + threadIdx.x; qd < quads;
+       qd += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(qd / (half / 4)), k0 = (int)(qd - (long long)i * (half / 4)) * 4, q = (i + c) & 1;
+    const uint8_t* up = Oc + (size_t)((i - 1) & (L - 1)) * half;
+    const uint8_t* dn = Oc + (size_t)((i + 1) & (L - 1)) * half;
+    const uint8_t* mid = Oc + (size_t)i * half;
+    uint8_t* row = Cc + (size_t)i * half;
+    uint32_t m4[4], tv4[4];
+    bool draw = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = k0 + j;
+      const uint32_t tv = row[k];
+      m4[j] = (up[k] != tv) + (dn[k] != tv) + (mid[(k - 1 + q) & (half - 1)] != tv) + (mid[(k + q) & (half - 1)] != tv);
+      tv4[j] = tv;
+      draw |= !((a.always_mask >> m4[j]) & 1u);
+    }
+    uint32_t flips = 0;
+    if (draw) {
+      const int w = k0 >> 5;
+      const uint4 A = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w), t);
+      const uint4 B = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w + 1), t);
+      const uint4 lo = stream_block(key, rep, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 2), t);
+      const uint32_t W[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int p = (k0 + j) & 31, pos = 8 * (p & 3) + (p >> 2);
+        uint32_t r8 = 0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) r8 |= ((W[b] >> pos) & 1u) << (7 - b);
+        const uint32_t u32 = (r8 << 24) | (u4get(lo, j) & 0xFFFFFFu);
+        if (((a.always_mask >> m4[j]) & 1u) || u32 < a.thr[m4[j]]) flips |= 1u << j;
+      }
+    } else {
+      flips = 0xFu;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if ((flips >> j) & 1u) row[k0 + j] = (uint8_t)(tv4[j] ^ 1u);
+  }
+}
+
 // Coupling sums of one HBM-resident level (and its blocking into the next).
 __global__ void __launch_bounds__(256) level_kernel(const uint8_t* __restrict__ in, int n, uint8_t* __restrict__ out,
                                                     unsigned long long* __restrict__ S, int C, Key key, uint32_t rep,
@@ -224,8 +280,7 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
   t->C = C;
   t->key = key;
   t->replica = replica;
-  t->acc = acc;
-  if (!acc.fast) return MCRG_ENOSYS;  // the tiled sweep implements the K < -ln2/4 fast path only
+  t->acc = acc;  // outside the fast regime the sweeps take the exact per-site path (exact_colour_kernel)
   {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -262,7 +317,6 @@ int tiled_alloc(TiledLattice* t, int L, int nl, int C, Key key, uint32_t replica
 }
 
 int tiled_reinit(TiledLattice* t, Key key, uint32_t replica, const Accept& acc, cudaStream_t s) {
-  if (!acc.fast) return MCRG_ENOSYS;
   t->key = key;
   t->replica = replica;
   t->acc = acc;
@@ -351,6 +405,14 @@ int tiled_variant(TiledLattice* t, int* rows, int* threads) {
 
 int tiled_sweeps(TiledLattice* t, uint32_t t0, int64_t n, cudaStream_t s) {
   if (n <= 0) return MCRG_OK;
+  if (!t->acc.fast) {  // two in-place colour passes per sweep
+    int grid = (int)(((long long)t->L * t->L / 8 + 255) / 256);
+    if (grid > t->sms * 8) grid = t->sms * 8;
+    for (int64_t k = 0; k < n; ++k)
+      for (int c = 0; c < 2; ++c)
+        exact_colour_kernel<<<grid, 256, 0, s>>>(t->buf[t->cur], t->L, c, t0 + (uint32_t)k, t->key, t->replica, t->acc);
+    return cudaGetLastError() == cudaSuccess ? MCRG_OK : MCRG_EIO;
+  }
   if (t->variant < 0) {
     t->variant = autotune(t, s);
     if (t->variant < 0) return MCRG_ENOSYS;

@@ -101,7 +101,7 @@ def test_cluster_update_bit_exact(M, L, kind):
     lattices (L <= 32), tiles merged across edges (L >= 64), shared-memory and HBM
     contexts (L >= 512), couplings with small, critical and percolating clusters and
     none (K > 0)."""
-    Ks = (KC, -0.3, -0.7, 0.2) if L <= 256 else (KC, -0.7)  # HBM contexts: fast acceptance regime only
+    Ks = (KC, -0.3, -0.7, 0.2)  # -0.3 and 0.2: outside the fast acceptance regime (exact sweeps)
     n = 4 if L <= 512 else 2
     for q, K in enumerate(Ks):
         seed, rep = 17 + L + q, 2

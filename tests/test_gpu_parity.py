@@ -94,10 +94,11 @@ def test_sweeps_bit_exact(M, N, K):
     lat.close()
 
 
-@pytest.mark.parametrize("N", [4, 8, 16, 32, 64, 256])
+@pytest.mark.parametrize("N", [4, 8, 16, 32, 64, 256, 512, 2048])
 @pytest.mark.parametrize("K", [-0.1, 0.0, 0.3])
 def test_sweeps_general_coupling(M, N, K):
-    """Couplings outside the fast path (K > -ln2/4) use the exact per-site rule."""
+    """Couplings outside the fast path (K > -ln2/4) use the exact per-site rule, in shared
+    memory (N <= 256) and on HBM lattices (two in-place colour passes per sweep)."""
     lat = M.Lattice(N, K, seed=3, replica=1)
     lat.sweep(4)
     ref = O.sweep(O.init_spins(N, 3, 1), K, 3, 1, 0, 4)
@@ -205,6 +206,20 @@ def test_measure_bit_exact(M, N, C, ns, sb):
     trace2, _ = O.chain(N, KC, C, nl, seed, rep, n_eq=0, n_samples=2, sweeps_between=1, spins=fin,
                         t0=n_eq + ns * sb, n0=ns)
     assert_moments_equal(tot2, MomentSums.from_trace(trace2))
+    lat.close()
+
+
+@pytest.mark.parametrize("K", [-0.1, 0.25])
+def test_hbm_measure_general_coupling(M, K):
+    """An HBM lattice outside the fast regime: sweeps, blocking, coupling sums and moments
+    equal the oracle's chain."""
+    N, C, nl = 1024, 3, 9
+    lat = M.Lattice(N, K, seed=21, replica=4, n_couplings=C)
+    lat.sweep(2)
+    tot, _ = lat.measure(3, 2)
+    trace, fin = O.chain(N, K, C, nl, 21, 4, n_eq=2, n_samples=3, sweeps_between=2)
+    assert_moments_equal(tot, MomentSums.from_trace(trace))
+    np.testing.assert_array_equal(lat.spins_, fin)
     lat.close()
 
 
