@@ -346,12 +346,27 @@ int mcrg_batch_stats(int32_t device, int64_t* launches, int64_t* graph_builds);
 /* ---------------------------------------------------------------------- */
 /* Serving: continuous batching of MCRG requests.                          */
 /* ---------------------------------------------------------------------- */
+/* A server admits requests in arrival order as slots and memory free up and
+ * runs them while others run.  Requests that fit a shared-memory-resident
+ * chain go, packed by shape, into a ring in page-locked host memory that a
+ * device-resident loop of persistent CTAs drains (one CTA per SM, relaunched
+ * when it has gone idle for 20 ms); their moments are written straight to
+ * page-locked host memory.  The others run on host worker threads, each on a
+ * context built inside the request's share of the arena.  The arena of
+ * hbm_budget_bytes is allocated once at creation and is all the device
+ * memory the server uses for requests: a request is charged every device
+ * byte it holds (the final configuration of a resident chain, the whole
+ * context of an HBM-path request), and waits while the budget is spent.  A
+ * result depends only on its request's seed and replica, never on what ran
+ * beside it.  No counterpart in the reference (it runs one chain per MPI
+ * rank, src/mcrg.cpp:42). */
 typedef struct {
   int32_t device;
-  int32_t slots;            /* concurrent resident chains (CTAs) */
-  int64_t hbm_budget_bytes; /* device bytes the server may hold for lattices */
+  int32_t slots;            /* resident chains admitted at a time (host result slots) */
+  int64_t hbm_budget_bytes; /* device bytes the server may hold for requests (one arena) */
   int32_t queue_capacity;   /* pending requests before mcrg_submit returns EBUSY */
-  int32_t hbm_workers;      /* host threads running HBM-size requests (L > MCRG_SMEM_MAX_L) concurrently;
+  int32_t hbm_workers;      /* host threads running requests no resident chain holds (L > 1024, or
+                               other acceptance regimes above MCRG_SMEM_MAX_L) concurrently;
                                0 selects 16, at most 256 */
 } mcrg_server_cfg;
 

@@ -35,7 +35,7 @@ struct mcrg_ctx {
   int* d_flag = nullptr;
   Accept acc;
   double* d_rgnn = nullptr;     // forward-pass work: (L/32)^2 + (L/1024)^2 + 3 doubles, the last one the result
-  int* d_labels = nullptr;      // cluster updates: L^2 labels (allocated by the first update)
+  int* d_labels = nullptr;      // cluster updates: L^2 labels + tile-edge bond masks (allocated by the first update)
   unsigned long long* d_cl = nullptr;  // cluster updates: [0] flipped spins, [1] error flags
   mcrg_moments* d_cbins = nullptr;     // cluster measurement: one bin per sample of a chunk
   ChainJob* d_cjobs = nullptr;         // cluster measurement: one measurement job per sample of a chunk
@@ -354,7 +354,7 @@ size_t context_bytes(int L, int n_levels, int C, int update, int64_t n_samples) 
   }
   b += a(sizeof(mcrg_moments) * (size_t)nb);  // the context's bins
   if (update)  // labels, counters, one chunk of per-sample bins and measurement jobs
-    b += a(sizeof(int) * LL) + a(2 * sizeof(unsigned long long)) + a(sizeof(mcrg_moments) * 256) +
+    b += a(sizeof(int) * cluster_label_ints(L)) + a(2 * sizeof(unsigned long long)) + a(sizeof(mcrg_moments) * 256) +
          a(sizeof(ChainJob) * 256);
   (void)n_levels;
   (void)C;
@@ -577,7 +577,7 @@ int mcrg_measure(mcrg_ctx* c, int64_t n_samples, int64_t sweeps_between, mcrg_mo
 static int cluster_updates(mcrg_ctx* c, int64_t n, int32_t kind) {
   const int L = c->cfg.L;
   if (!c->d_labels) {
-    if (dev_alloc(c->span, &c->d_labels, sizeof(int) * (size_t)L * L) != cudaSuccess) return MCRG_ENOMEM;
+    if (dev_alloc(c->span, &c->d_labels, sizeof(int) * cluster_label_ints(L)) != cudaSuccess) return MCRG_ENOMEM;
     if (dev_alloc(c->span, &c->d_cl, 2 * sizeof(unsigned long long)) != cudaSuccess) {
       dev_release(c->span, c->d_labels);
       c->d_labels = nullptr;

@@ -16,11 +16,15 @@
 //      every site points at the first site of its run (count leading zeros),
 //      and only vertical bonds are united, one per pair of runs, taken by
 //      all threads from one list for the whole tile;
-//   2. cl_merge_kernel (L > 32): every open bond that crosses a tile edge
-//      unites the two trees of the global forest; atomicMin links the larger
-//      root under the smaller, so a root is always the smallest index of its
-//      tree and, at the end, of its cluster (finds halve the paths they walk:
-//      a cluster spanning thousands of tiles would otherwise leave long chains);
+//      It also records, as two 32-bit masks per tile, which of its bonds into
+//      the next tiles (right of column 31, below row 31) are open: it draws
+//      them anyway and holds the spins on both sides;
+//   2. cl_merge_kernel (L > 32): every open bond that crosses a tile edge (a
+//      set mask bit) unites the two trees of the global forest; atomicMin
+//      links the larger root under the smaller, so a root is always the
+//      smallest index of its tree and, at the end, of its cluster (finds halve
+//      the paths they walk: a cluster spanning thousands of tiles would
+//      otherwise leave long chains);
 //   3. cl_flip_kernel: every site finds its root; Wolff flips the sites that
 //      share the seed's root, Swendsen-Wang the sites whose root draws a set
 //      bit; the flips are counted.  With T = 32 a CTA loads its tile's labels
@@ -147,24 +151,37 @@ __global__ void __launch_bounds__(256) cl_tile_kernel(const uint8_t* __restrict_
 
 // Tiles of 32 x 32 (L >= 32): warp w owns rows w, w+8, w+16, w+24.  Sites
 // point at the first site of their horizontal run; vertical bonds unite runs.
+// Besides the in-tile labels it records the tile's bonds into the next tiles
+// (L > 32), whose draws it makes anyway: edges[2 tile] bit r = the right bond
+// of (i0 + r, j0 + 31), edges[2 tile + 1] bit c = the down bond of
+// (i0 + 31, j0 + c).  The merge then reads these masks instead of drawing the
+// bonds and reading the spins again.
 __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restrict__ st, int L,
-                                                        int* __restrict__ label, Key key, uint32_t rep, uint32_t t,
-                                                        uint32_t tb, int* err) {
+                                                        int* __restrict__ label, uint32_t* __restrict__ edges,
+                                                        Key key, uint32_t rep, uint32_t t, uint32_t tb, int* err) {
   __shared__ int par[1024];
   __shared__ uint8_t sp[33 * 32];  // spins of the tile's rows and of the row below it
-  __shared__ uint32_t hb[32], vb[32];
+  __shared__ uint8_t ecol[32];     // spins of column j0 + 32 (the next tile's first column)
+  __shared__ uint32_t hb[32], vb[32], redge;
   __shared__ int vlist[1024], nv;  // vertical bonds that join two runs, as their upper site
   const int tpr = L >> 5, ti = blockIdx.x / tpr, tj = blockIdx.x - ti * tpr;
   const int i0 = ti << 5, j0 = tj << 5, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool one = L == 32;  // a one-tile lattice: its wrap bonds are in-tile bonds
-  if (threadIdx.x == 0) nv = 0;
+  const int h = L / 2;
+  if (threadIdx.x == 0) {
+    nv = 0;
+    redge = 0;
+  }
   if (threadIdx.x < 66) {  // 33 rows x 2 colours: 16 bytes each, de-interleaved into natural order
-    const int r = threadIdx.x >> 1, c = threadIdx.x & 1, i = (i0 + r) & (L - 1), h = L / 2;
+    const int r = threadIdx.x >> 1, c = threadIdx.x & 1, i = (i0 + r) & (L - 1);
     const uint4 v = *reinterpret_cast<const uint4*>(st + (size_t)c * L * h + (size_t)i * h + (j0 >> 1));
     const uint32_t w[4] = {v.x, v.y, v.z, v.w};
     const int q = (i + c) & 1;  // column parity of colour c in row i (j0 is even)
 #pragma unroll
     for (int b = 0; b < 16; ++b) sp[r * 32 + 2 * b + q] = (uint8_t)((w[b >> 2] >> (8 * (b & 3))) & 0xFFu);
+  } else if (threadIdx.x >= 96 && threadIdx.x < 128 && !one) {  // site (i, j0 + 32): colour i & 1 (j0 + 32 is even)
+    const int r = threadIdx.x - 96, i = i0 + r;
+    ecol[r] = st[(size_t)(i & 1) * L * h + (size_t)i * h + (((j0 + 32) & (L - 1)) >> 1)];
   }
   __syncthreads();
   for (int rp = warp; rp < 16; rp += 8) {  // row pairs 2rp, 2rp+1: lane l draws pair l & 15 of row 2rp + (l >> 4)
@@ -180,6 +197,13 @@ __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restric
       const bool right = ur < tb && (lane < 31 || one) && sp[r * 32 + ((lane + 1) & 31)] == s;
       const bool down = ud < tb && (r < 31 || one) && sp[(r + 1) * 32 + lane] == s;
       const uint32_t hm = __ballot_sync(0xFFFFFFFFu, right), vm = __ballot_sync(0xFFFFFFFFu, down);
+      if (!one) {  // the bonds into the next tiles: right of column 31, below row 31
+        if (lane == 31 && ur < tb && ecol[r] == s) atomicOr(&redge, 1u << r);
+        if (r == 31) {
+          const uint32_t dm = __ballot_sync(0xFFFFFFFFu, ud < tb && sp[32 * 32 + lane] == s);
+          if (lane == 0) edges[2 * (size_t)blockIdx.x + 1] = dm;
+        }
+      }
       const uint32_t starts = ~(hm << 1);  // bit c: the bond (c-1, c) is closed (bit 0 always); the wrap bit drops out
       const uint32_t low = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
       par[r * 32 + lane] = r * 32 + (31 - __clz(starts & low));
@@ -203,6 +227,7 @@ __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restric
     if ((m >> lane) & 1u) vlist[base + __popc(m & ((1u << lane) - 1u))] = r * 32 + lane;
   }
   __syncthreads();
+  if (!one && threadIdx.x == 0) edges[2 * (size_t)blockIdx.x] = redge;
   for (int e = threadIdx.x; e < nv; e += 256) {
     const int x = vlist[e];
     unite<true>(par, x, (x + 32) & 1023, err);
@@ -216,26 +241,27 @@ __global__ void __launch_bounds__(256) cl_tile32_kernel(const uint8_t* __restric
   }
 }
 
-// Open bonds that cross a tile edge (L > kTile): the right bonds of column
-// T-1 and the down bonds of row T-1 of every tile (periodic wrap included).
-__global__ void __launch_bounds__(256) cl_merge_kernel(const uint8_t* __restrict__ st, int L, int* label, Key key,
-                                                       uint32_t rep, uint32_t t, uint32_t tb, int* err) {
+// Open bonds that cross a tile edge (L > kTile), from the masks the tile
+// kernel recorded: the right bonds of column 31 and the down bonds of row 31
+// of every tile (periodic wrap included).  One thread per mask bit; a warp
+// reads one mask.
+__global__ void __launch_bounds__(256) cl_merge_kernel(const uint32_t* __restrict__ edges, int L, int* label,
+                                                       int* err) {
   const int tpr = L / kTile, m = L - 1;
-  const long long right = (long long)L * tpr, total = 2 * right;
+  const long long total = 64LL * tpr * tpr;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
-    if (e < right) {
-      const int i = (int)(e / tpr), j = (int)(e - (long long)i * tpr) * kTile + kTile - 1;  // odd
-      const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j >> 1), t);
-      if (r.z < tb && nat_spin(st, L, i, j) == nat_spin(st, L, i, (j + 1) & m))
-        unite<true>(label, i * L + j, i * L + ((j + 1) & m), err);
+    const long long tile = e >> 6;
+    const int b = (int)(e & 63), k = b & 31;
+    if (!((edges[2 * tile + (b >> 5)] >> k) & 1u)) continue;
+    const int ti = (int)(tile / tpr), tj = (int)(tile - (long long)ti * tpr);
+    const int i0 = ti * kTile, j0 = tj * kTile;
+    if (b < 32) {
+      const int i = i0 + k, j = j0 + kTile - 1;
+      unite<true>(label, i * L + j, i * L + ((j + 1) & m), err);
     } else {
-      const long long e2 = e - right;
-      const int i = (int)(e2 / L) * kTile + kTile - 1, j = (int)(e2 - (e2 / L) * L);
-      const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j >> 1), t);
-      const uint32_t u = (j & 1) ? r.w : r.y;
-      if (u < tb && nat_spin(st, L, i, j) == nat_spin(st, L, (i + 1) & m, j))
-        unite<true>(label, i * L + j, ((i + 1) & m) * L + j, err);
+      const int i = i0 + kTile - 1, j = j0 + k;
+      unite<true>(label, i * L + j, ((i + 1) & m) * L + j, err);
     }
   }
 }
@@ -378,15 +404,16 @@ cudaError_t launch_cluster_update(uint8_t* d_state, int L, int* d_label, int kin
                                   uint32_t t, uint32_t bond_threshold, unsigned long long* d_count, int* d_err,
                                   int num_sms, cudaStream_t s) {
   const int T = L < kTile ? L : kTile, tiles = (L / T) * (L / T);
+  uint32_t* edges = reinterpret_cast<uint32_t*>(d_label + (size_t)L * L);  // 2 masks per tile
   if (L >= kTile)
-    cl_tile32_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
+    cl_tile32_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, edges, key, replica, t, bond_threshold, d_err);
   else
     cl_tile_kernel<<<tiles, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
   if (L > kTile) {
-    const long long edges = 2LL * L * (L / kTile);
-    long long blocks = (edges + 255) / 256;
+    const long long bits = 64LL * tiles;
+    long long blocks = (bits + 255) / 256;
     if (blocks > 8LL * num_sms) blocks = 8LL * num_sms;
-    cl_merge_kernel<<<(int)blocks, 256, 0, s>>>(d_state, L, d_label, key, replica, t, bond_threshold, d_err);
+    cl_merge_kernel<<<(int)blocks, 256, 0, s>>>(edges, L, d_label, d_err);
   }
   if (L >= kTile) {
     int lg = 0;

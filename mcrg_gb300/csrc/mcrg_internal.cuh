@@ -205,12 +205,14 @@ cudaError_t launch_couplings_once(const uint8_t* d_in, int N, int C, int* d_out,
 cudaError_t launch_nat_to_split(const int8_t* d_nat, int N, uint8_t* d_split, int* d_bad, cudaStream_t s);
 
 // One cluster update (Wolff or Swendsen-Wang, mcrg_cluster.cu) of a split-
-// layout lattice of side L at update index t: d_label holds L^2 ints,
+// layout lattice of side L at update index t: d_label holds
+// cluster_label_ints(L) ints (L^2 labels, then two bond masks per 32 x 32 tile),
 // *d_count gains the number of flipped spins, *d_err gets bit 2 / 4 when a
 // find / union loop hits its bound.
 cudaError_t launch_cluster_update(uint8_t* d_state, int L, int* d_label, int kind, Key key, uint32_t replica,
                                   uint32_t t, uint32_t bond_threshold, unsigned long long* d_count, int* d_err,
                                   int num_sms, cudaStream_t s);
+inline size_t cluster_label_ints(int L) { return (size_t)L * L + (size_t)L * L / 512 + 2; }
 // floor((1 - exp(2K)) 2^32), 0 when no bond can open (K >= 0).
 uint32_t bond_threshold(double K);
 
