@@ -173,9 +173,9 @@ def peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profiled_traffic(name: str):
-    """Per-launch DRAM bytes of a kernel from a committed ncu summary line
-    'traffic_bytes_per_launch <kernel> <workload> <bytes>' in profiles/."""
+def profiled(key: str, name: str):
+    """A figure of a kernel from a committed ncu summary line
+    '<key> <kernel> <workload> <value>' in profiles/ (None when absent)."""
     d = os.path.join(ROOT, "profiles")
     try:
         for fn in sorted(os.listdir(d)):
@@ -183,11 +183,17 @@ def profiled_traffic(name: str):
                 continue
             for ln in open(os.path.join(d, fn)):
                 f = ln.split()
-                if len(f) == 4 and f[0] == "traffic_bytes_per_launch" and f[1] == name:
-                    return int(float(f[3]))
+                if len(f) == 4 and f[0] == key and f[1] == name:
+                    return float(f[3])
     except Exception:
         pass
     return None
+
+
+def profiled_traffic(name: str):
+    """Per-launch DRAM bytes of a kernel ('traffic_bytes_per_launch' lines)."""
+    v = profiled("traffic_bytes_per_launch", name)
+    return None if v is None else int(v)
 
 
 # ---------------------------------------------------------------------------
@@ -398,6 +404,9 @@ def batched_cfg(args, D: Dist) -> dict:
             "equal_error": "same seeds: batched and plain runs give bit-identical moment sums, so identical "
                            "T-eigenvalue estimates and error bars (checked on the timed plain requests)",
             "threads_per_chain": sched, "graph_builds": st["graph_builds"], "launches": st["launches"],
+            "roofline": {"bound": "sm_issue", "kernel": "pool_kernel<256,3>",
+                         "issue_active_frac": profiled("issue_active_frac", "pool_kernel_batched"),
+                         "source": "ncu, profiles/pool_kernel_batched.md (200-sweep batch of the same mix)"},
             "clocks": clocks,
             "config": {"workload": "batched: %d replicas in one persistent launch, L in {16..256} (p = .3/.3/.2/.15/"
                                    ".05), K on 33 points in [-0.49,-0.43], %d %s each measured after every one, "
@@ -800,7 +809,7 @@ def main():
     ap.add_argument("--cluster-equilibrate", type=int, default=60, help="cluster workload: SW updates first")
     ap.add_argument("--plain-per-side", type=int, default=2, help="plain-path requests timed per lattice side")
     ap.add_argument("--plain-sweeps", type=int, default=10000)
-    ap.add_argument("--served-requests", type=int, default=2000)
+    ap.add_argument("--served-requests", type=int, default=4000)
     ap.add_argument("--served-scale", type=float, default=1.0, help="sweeps of the served mix x this (1: as stated)")
     ap.add_argument("--served-slots", type=int, default=1024)
     ap.add_argument("--served-budget-gb", type=float, default=150.0)

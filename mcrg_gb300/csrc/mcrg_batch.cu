@@ -178,6 +178,10 @@ struct Candidate {
   int threads = 0;
   double s_sample = 0;
   double rate = 0;
+  // the same chains inside 512-wide CTAs (the width a batch takes when any of
+  // its shapes runs 512 threads per chain); 0 when not timed or not fitting
+  double s_sample512 = 0;
+  double rate512 = 0;
 };
 
 struct Schedule {
@@ -372,8 +376,7 @@ size_t queue_bytes(size_t n_packs, size_t n_jobs) {
 // One trial of the autotuner: a full wave of chains of one shape at `g`
 // threads each, S samples per chain; returns seconds per sample of a chain
 // (the wave's time / S) or -1 when the shape does not fit that way.
-double trial_pool(BatchWorkspace& w, int L, int nl, int C, int mode, int g) {
-  const int W = g > 256 ? 512 : 256;
+double trial_pool(BatchWorkspace& w, int L, int nl, int C, int mode, int g, int W) {
   int m = 0, stride = 0, occ = 0;
   if (!pack_geometry(L, nl, C, mode, g, W, &m, &stride)) return -1;
   if (pool_prepare(W, m * stride, &occ) != cudaSuccess || occ < 1) return -1;
@@ -455,16 +458,31 @@ Schedule schedule_for(BatchWorkspace& w, int device, int L, int nl, int C, int m
   }
   Schedule best;
   double best_rate = -1;
-  for (int g : candidate_threads(L, mode)) {
-    if (forced && g != forced) continue;
-    const double t = trial_pool(w, L, nl, C, mode, g);
-    if (t <= 0) continue;
+  // chain samples per second of the device running only this shape at width W
+  auto device_rate = [&](int g, int W, double t) {
     int m = 0, stride = 0, occ = 0;
-    const int W = g > 256 ? 512 : 256;
     pack_geometry(L, nl, C, mode, g, W, &m, &stride);
     pool_prepare(W, m * stride, &occ);
-    const double rate = (double)w.sms * occ * m / t;  // chain samples per second over the device
-    best.cand.push_back(Candidate{g, t, rate});
+    return (double)w.sms * occ * m / t;
+  };
+  for (int g : candidate_threads(L, mode)) {
+    if (forced && g != forced) continue;
+    const int W = g > 256 ? 512 : 256;
+    const double t = trial_pool(w, L, nl, C, mode, g, W);
+    if (t <= 0) continue;
+    Candidate cd{g, t, device_rate(g, W, t), 0, 0};
+    if (W == 512) {
+      cd.s_sample512 = cd.s_sample;
+      cd.rate512 = cd.rate;
+    } else {
+      const double t5 = trial_pool(w, L, nl, C, mode, g, 512);
+      if (t5 > 0) {
+        cd.s_sample512 = t5;
+        cd.rate512 = device_rate(g, 512, t5);
+      }
+    }
+    const double rate = cd.rate;
+    best.cand.push_back(cd);
     if (rate > best_rate) {
       best_rate = rate;
       best.threads = g;
@@ -474,7 +492,7 @@ Schedule schedule_for(BatchWorkspace& w, int device, int L, int nl, int C, int m
   if (!best.threads) {  // nothing fit (should not happen for resident shapes): the fixed rule
     best.threads = resident_threads(L, (mode & 2) != 0);
     best.s_sample = 0;
-    best.cand.push_back(Candidate{best.threads, 0.0, 0.0});
+    best.cand.push_back(Candidate{best.threads, 0.0, 0.0, 0.0, 0.0});
   }
   if (forced) return best;
   if (tiled_candidate(L, mode)) best.s_tiled = trial_tiled(device, L, nl, C);
@@ -496,11 +514,13 @@ double chain_samples(const mcrg_request& q) {
   return (double)q.n_samples + 0.5 * sweeps;
 }
 
-// Threads per chain for every shape of a batch: the combination of timed
-// candidates with the smallest estimated makespan, max(longest chain at its
-// latency under load, total work at each shape's device throughput) -- the
-// best-throughput candidate alone can leave the batch waiting on a few long,
-// narrow chains.
+// Threads per chain for every shape of a batch, and so the CTA width: the
+// combination of timed candidates with the smallest estimated makespan,
+// max(longest chain × its latency, Σ work / throughput), each shape's
+// latency and throughput taken at the width the combination implies (512
+// when any shape runs 512 threads per chain, else 256) -- the best-throughput
+// pick alone can leave the batch waiting on a few long, narrow chains, and a
+// 512-wide launch slows the shapes that did not need it.
 void choose_threads(std::vector<Shape>& sh, const std::vector<std::vector<Candidate>>& cands,
                     const mcrg_request* reqs) {
   const size_t n = sh.size();
@@ -517,13 +537,16 @@ void choose_threads(std::vector<Shape>& sh, const std::vector<std::vector<Candid
   std::vector<size_t> pick(n, 0), best(n, 0);
   double best_t = -1;
   for (;;) {
+    bool wide = false;
+    for (size_t k = 0; k < n; ++k) wide |= cands[k][pick[k]].threads > 256;
     double lat = 0, thr = 0;
     bool ok = true;
     for (size_t k = 0; k < n; ++k) {
       const Candidate& c = cands[k][pick[k]];
-      if (c.rate <= 0) ok = false;
-      lat = std::max(lat, longest[k] * c.s_sample);
-      thr += c.rate > 0 ? total[k] / c.rate : 0;
+      const double sr = wide ? c.s_sample512 : c.s_sample, rt = wide ? c.rate512 : c.rate;
+      if (rt <= 0 || sr <= 0) ok = false;
+      lat = std::max(lat, longest[k] * sr);
+      thr += rt > 0 ? total[k] / rt : 0;
     }
     const double t = std::max(lat, thr);
     if (ok && (best_t < 0 || t < best_t)) {

@@ -374,8 +374,11 @@ cudaError_t serve_prepare(int smem, int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, serve_kernel, kServeThreads, smem);
 }
 
+// The 512-wide instantiation runs one CTA per SM: held to 64 registers for
+// two, the chain code spills (measured 6-7 % slower on batches of cluster
+// chains).
 const void* pool_kernel_fn(int cta_threads) {
-  return cta_threads > 256 ? (const void*)pool_kernel<512, 2> : (const void*)pool_kernel<256, 3>;
+  return cta_threads > 256 ? (const void*)pool_kernel<512, 1> : (const void*)pool_kernel<256, 3>;
 }
 
 cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm) {
@@ -391,7 +394,7 @@ cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm) {
     if (e != cudaSuccess) return e;
     configured[wide].fetch_or(bit, std::memory_order_release);
   }
-  return wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<512, 2>, cta_threads, smem)
+  return wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<512, 1>, cta_threads, smem)
               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<256, 3>, cta_threads, smem);
 }
 

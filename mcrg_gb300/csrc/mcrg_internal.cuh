@@ -189,7 +189,7 @@ const void* serve_kernel_fn();
 // CTAs per SM for `smem` bytes.
 cudaError_t serve_prepare(int smem, int* blocks_per_sm);
 
-// CTA widths of the pool kernel: 256 (3 CTAs per SM by registers) or 512.
+// CTA widths of the pool kernel: 256 (3 CTAs per SM by registers) or 512 (one per SM).
 const void* pool_kernel_fn(int cta_threads);
 // Sets the kernel's shared-memory limit (once per device) and returns its
 // resident CTAs per SM for `smem` bytes of dynamic shared memory.
