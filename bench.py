@@ -8,7 +8,7 @@ coupling sums, exact int128 moment products).  Metric: Gflips/s = L^2 *
 sweeps / s (site updates).  The lattice (268 MB) is larger than L2 (129 MB),
 so no L2 flush is needed between steps.
 
-The same line carries, at N = 1, three sub-objects measured in the same run,
+The same line carries, at N = 1, four sub-objects measured in the same run,
 each with its own clock record:
   "batched": 4096 replicas in one persistent launch (L from {16..256} with
              p = .3/.3/.2/.15/.05, K on 33 points in [-0.49, -0.43], 1e5
@@ -20,7 +20,10 @@ each with its own clock record:
              solves/s, against the plain path on the same mix;
   "config1": the reference's CPU-runnable solve (L = 8, 1e4 + 1e5 sweeps, 2
              levels) as MCRG solves/s: plain GPU, batched GPU, and the
-             reference's Wolff path on every host core.
+             reference's Wolff path on every host core;
+  "config2": the plain GPU configuration (L = 64, 2e4 + 1e6 sweeps, 5
+             couplings) against 1000 batched replicas with the same number
+             of samples: time and jackknife errors of the T eigenvalues.
 
 Other workloads (--workload): "batched", "served", "plain" (one L = 64
 lattice, one CTA per launch), "cluster" (Wolff / Swendsen-Wang updates of one
@@ -496,6 +499,57 @@ def served_cfg(args, D: Dist) -> dict:
                                 % args.plain_per_side}}
 
 
+def config2_cfg(args, D: Dist) -> dict:
+    """Config "plain GPU path" (one L = 64 lattice, K = Kc, 5 couplings, 5 levels,
+    2e4 thermalisation + 1e6 measured sweeps, binned error bars) against the same
+    statistics from the batched form: 1000 independent replicas of 2e4 + 1000
+    sweeps in one batch (1e6 samples in all).  Both give the leading T eigenvalue
+    per level with a jackknife error over 100 bins (10^4 consecutive samples of
+    the plain chain; 10 replicas of the batch), so the speed-up is quoted at
+    equal statistical error, which the error ratio shows."""
+    import numpy as np
+    import torch
+    import mcrg_gb300 as M
+    from mcrg_gb300.tmatrix import jackknife
+    dev = D.local
+    torch.cuda.set_device(dev)
+    n_eq, n_s, C_, R = 20000, 1000000, 5, 1000
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat = M.Lattice(64, KC, seed=1, replica=0, n_couplings=C_, device=dev)
+    lat.sweep(n_eq)
+    _, bins = lat.measure(n_s, 1, bin_size=n_s // 100)
+    lat.close()
+    t_plain = time.perf_counter() - t0
+    lam_p, err_p = jackknife(bins)
+    reqs = [M.make_request(64, KC, seed=1, replica=1 + i, n_eq=n_eq, n_samples=n_s // R, n_couplings=C_)
+            for i in range(R)]
+    M.batch_schedule(reqs[0], dev)  # schedule trials before the timed batch
+    creqs = (M._abi.Request * R)(*reqs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = M.batch_run(creqs, device=dev, raw=True)
+    t_batch = time.perf_counter() - t0
+    assert all(r.status == 0 for r in res)
+    ms = [M.moments_from_c(r.moments) for r in res]
+    groups = []
+    for g in range(100):
+        tot = ms[g * (R // 100)]
+        for m in ms[g * (R // 100) + 1:(g + 1) * (R // 100)]:
+            tot = tot + m
+        groups.append(tot)
+    lam_b, err_b = jackknife(groups)
+    return {"plain": {"seconds": round(t_plain, 3), "lambda": [round(x, 5) for x in lam_p],
+                      "lambda_err": [round(x, 5) for x in err_p]},
+            "batched": {"seconds": round(t_batch, 3), "replicas": R, "lambda": [round(x, 5) for x in lam_b],
+                        "lambda_err": [round(x, 5) for x in err_b]},
+            "speedup_at_equal_samples": round(t_plain / t_batch, 1),
+            "error_ratio_batched_over_plain": [round(b / p, 3) if p > 0 else None for b, p in zip(err_b, err_p)],
+            "config": {"workload": "config 2: L=64, K=Kc, 5 couplings, 5 levels; plain = one chain of 2e4 + 1e6 "
+                                   "sweeps (one CTA); batched = 1000 replicas of 2e4 + 1000 sweeps in one launch; "
+                                   "jackknife errors over 100 bins each"}}
+
+
 def config1_cfg(args, D: Dist) -> dict:
     """The reference's CPU-runnable solve (L = 8, K = Kc, 1e4 + 1e5 sweeps, 2 levels,
     2 couplings) as MCRG solves/s: plain GPU (one context), batched GPU (--replicas
@@ -835,6 +889,7 @@ def main():
         out["batched"] = batched_cfg(args, D)
         out["served"] = served_cfg(args, D)
         out["config1"] = config1_cfg(args, D)
+        out["config2"] = config2_cfg(args, D)
     if D.rank == 0 and D.world == 1 and not args.no_cpu_baseline and args.workload != "cluster":
         threads, why = cpu_threads(args.L if args.workload == "large" else 64)
         cb = cpu_reference(args.L if args.workload == "large" else 64, args.cpu_seconds, threads, args.couplings)
