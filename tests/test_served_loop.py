@@ -136,3 +136,29 @@ def test_request_larger_than_budget_is_refused(M):
         assert e.value.code == _abi.ENOSPC
     finally:
         srv.close()
+
+
+def test_hbm_path_requests_at_any_coupling(M):
+    """Requests no resident chain holds run on the worker threads: L = 512 / 1024
+    outside the fast acceptance regime (exact HBM sweeps), cluster updates at L = 512,
+    and L = 2048; each result equals its single-context run, in the mix with resident
+    requests, in the batch as in the server."""
+    reqs = [M.make_request(512, -0.1, seed=71, replica=1, n_eq=2, n_samples=2, n_couplings=3),
+            M.make_request(1024, 0.2, seed=72, replica=2, n_eq=1, n_samples=2, n_couplings=2),
+            M.make_request(512, KC, seed=73, replica=3, n_eq=2, n_samples=2, n_couplings=2, update="wolff"),
+            M.make_request(512, -0.3, seed=74, replica=4, n_eq=1, n_samples=2, n_couplings=2, update="sw"),
+            M.make_request(2048, -0.45, seed=75, replica=5, n_eq=1, n_samples=1, n_couplings=2),
+            M.make_request(64, -0.46, seed=76, replica=6, n_eq=3, n_samples=4, n_couplings=5),
+            M.make_request(256, -0.1, seed=77, replica=7, n_eq=3, n_samples=3, n_couplings=2)]
+    want = [solo(M, r) for r in reqs]
+    srv = M.Server(slots=16, hbm_budget_bytes=512 << 20, hbm_workers=4)
+    try:
+        out = [srv.wait(t, 300) for t in [srv.submit(r) for r in reqs]]
+    finally:
+        srv.close()
+    for r, o, w in zip(reqs, out, want):
+        assert o.status == 0, (r.L, r.K, o.status)
+        assert same(M.moments_from_c(o.moments), w), (r.L, r.K, r.flags)
+    for r, (st, mom), w in zip(reqs, M.batch_run(reqs), want):
+        assert st == 0
+        assert same(mom, w), (r.L, r.K, r.flags)
