@@ -326,9 +326,13 @@ typedef struct {
  * the upload, clear, launch and download are one CUDA graph, instantiated
  * once per device, CTA width, grid and buffer set and re-launched with
  * updated copy sizes.  Requests that no chain holds run on the tiled HBM
- * path after the resident launch.  Environment: MCRG_POOL_THREADS=<n>
- * forces n threads per chain where n is a candidate; MCRG_BATCH_SCHEDULE=
- * resident | tiled forces the choice for the largest resident sides. */
+ * path after the resident launch.  The packs are queued by chain code (byte
+ * sweeps, plane sweeps, cluster updates) and each SM serves first the code
+ * its share of SM ids was given (shares by estimated work), so that the CTAs
+ * of one SM share their instructions in cache.  Environment:
+ * MCRG_POOL_THREADS=<n> forces n threads per chain where n is a candidate;
+ * MCRG_BATCH_SCHEDULE=resident | tiled forces the choice for the largest
+ * resident sides; MCRG_POOL_CLASSES=0 puts every pack in one queue. */
 int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* results, int32_t device,
                    int32_t use_graph);
 

@@ -354,15 +354,37 @@ BatchWorkspace& workspace(int device) {
 
 // Lays out [PoolQueue | packs | jobs] in the workspace's pinned staging with
 // device pointers, and returns the bytes used.
-size_t stage_queue(BatchWorkspace& w, const std::vector<PoolPack>& packs, const std::vector<ChainJob>& jobs) {
-  const size_t off_packs = 64;
+// The packs must be ordered by class; class_first[k] is the first pack of
+// class k (class_first[n] = packs.size()), class_work[k] its estimated work.
+size_t stage_queue(BatchWorkspace& w, const std::vector<PoolPack>& packs, const std::vector<ChainJob>& jobs,
+                   const std::vector<int>& class_first = {}, const std::vector<double>& class_work = {}) {
+  const size_t off_packs = 128;
   const size_t off_jobs = (off_packs + sizeof(PoolPack) * packs.size() + 255) & ~size_t(255);
+  static_assert(sizeof(PoolQueue) <= 128, "queue header");
   PoolQueue q;
   memset(&q, 0, sizeof q);
   q.n_packs = (int32_t)packs.size();
   q.packs = reinterpret_cast<const PoolPack*>(w.d_buf + off_packs);
   q.jobs = reinterpret_cast<const ChainJob*>(w.d_buf + off_jobs);
   q.next = reinterpret_cast<unsigned*>(w.d_out);
+  const char* pc = getenv("MCRG_POOL_CLASSES");
+  const bool classes = !(pc && pc[0] == '0') && class_first.size() >= 2;
+  if (!classes) {  // one class: every CTA takes every pack in order
+    q.n_classes = 1;
+    q.first[0] = 0;
+    q.first[1] = (int32_t)packs.size();
+  } else {
+    const int nc = std::min((int)class_first.size() - 1, kPoolClasses);
+    double tot = 0;
+    for (int k = 0; k < nc; ++k) tot += class_work[(size_t)k];
+    q.n_classes = nc;
+    double acc = 0;
+    for (int k = 0; k <= nc; ++k) {
+      q.first[k] = class_first[(size_t)k];
+      q.sm_edge[k] = (int32_t)(tot > 0 ? acc / tot * 65536.0 : 0.0);
+      if (k < nc) acc += class_work[(size_t)k];
+    }
+  }
   memcpy(w.h_buf, &q, sizeof q);
   if (!packs.empty()) memcpy(w.h_buf + off_packs, packs.data(), sizeof(PoolPack) * packs.size());
   if (!jobs.empty()) memcpy(w.h_buf + off_jobs, jobs.data(), sizeof(ChainJob) * jobs.size());
@@ -370,7 +392,7 @@ size_t stage_queue(BatchWorkspace& w, const std::vector<PoolPack>& packs, const 
 }
 
 size_t queue_bytes(size_t n_packs, size_t n_jobs) {
-  return ((64 + sizeof(PoolPack) * n_packs + 255) & ~size_t(255)) + sizeof(ChainJob) * n_jobs;
+  return ((128 + sizeof(PoolPack) * n_packs + 255) & ~size_t(255)) + sizeof(ChainJob) * n_jobs;
 }
 
 // One trial of the autotuner: a full wave of chains of one shape at `g`
@@ -627,7 +649,13 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
     size_t state_bytes = 0;
     int64_t total_bins = 0;
     int smem = 16;
-    std::vector<std::pair<double, PoolPack>> costed;
+    struct Costed {
+      int cls;      // chain code: 0 byte sweeps, 1 plane sweeps, 2 cluster updates
+      double cost;  // of the pack's longest chain
+      double work;  // of all its chains
+      PoolPack pk;
+    };
+    std::vector<Costed> costed;
     for (auto it = sh.begin(); it != sh.end();) {  // a shape no pack holds runs on the tiled path
       if (!pack_geometry(it->L, it->nl, it->C, it->mode, it->g, W, &it->per_pack, &it->stride)) {
         tiled.insert(tiled.end(), it->reqs.begin(), it->reqs.end());
@@ -643,9 +671,13 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         return (double)q.L * q.L * (double)(q.n_eq + q.n_samples * (q.sweeps_between + 1));
       };
       std::stable_sort(s.reqs.begin(), s.reqs.end(), [&](int a, int b) { return cost(a) > cost(b); });
+      const int cls = (s.mode & 2) ? 2 : (s.mode & 1);
       for (size_t k = 0; k < s.reqs.size(); k += (size_t)s.per_pack) {
         const int cnt = (int)std::min(s.reqs.size() - k, (size_t)s.per_pack);
-        costed.push_back({cost(s.reqs[k]), PoolPack{(int32_t)(jobs.size() + k), (int16_t)cnt, (int16_t)s.g, s.stride, 0}});
+        double work = 0;
+        for (int q = 0; q < cnt; ++q) work += cost(s.reqs[k + (size_t)q]);
+        costed.push_back({cls, cost(s.reqs[k]), work,
+                          PoolPack{(int32_t)(jobs.size() + k), (int16_t)cnt, (int16_t)s.g, s.stride, 0}});
       }
       for (int i : s.reqs) {
         state_off[i] = state_bytes;
@@ -657,12 +689,21 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
       }
       smem = std::max(smem, s.per_pack * s.stride);
     }
-    // longest packs first: the tail of the launch is short chains
-    std::stable_sort(costed.begin(), costed.end(),
-                     [](const std::pair<double, PoolPack>& a, const std::pair<double, PoolPack>& b) {
-                       return a.first > b.first;
-                     });
-    for (auto& c : costed) packs.push_back(c.second);
+    // by chain code, and longest packs first within each: the tail of the launch is short chains
+    std::stable_sort(costed.begin(), costed.end(), [](const Costed& a, const Costed& b) {
+      return a.cls != b.cls ? a.cls < b.cls : a.cost > b.cost;
+    });
+    std::vector<int> class_first;
+    std::vector<double> class_work;
+    for (size_t k = 0; k < costed.size(); ++k) {
+      if (k == 0 || costed[k].cls != costed[k - 1].cls) {
+        class_first.push_back((int)k);
+        class_work.push_back(0.0);
+      }
+      class_work.back() += costed[k].work;
+      packs.push_back(costed[k].pk);
+    }
+    class_first.push_back((int)costed.size());
     if (!rc && !jobs.empty()) {
       rc = w.reserve(state_bytes + 16, queue_bytes(packs.size(), jobs.size()), (size_t)std::max<int64_t>(total_bins, 1));
       if (!rc) {
@@ -676,7 +717,7 @@ extern "C" int mcrg_batch_run(const mcrg_request* reqs, int32_t n, mcrg_result* 
         int occ = 0;
         if (pool_prepare(W, smem, &occ) != cudaSuccess || occ < 1) rc = MCRG_EIO;
         const int grid = std::min((int)packs.size(), w.sms * std::max(occ, 1));
-        const size_t up = stage_queue(w, packs, jobs);
+        const size_t up = stage_queue(w, packs, jobs, class_first, class_work);
         if (!rc) rc = w.run(W, grid, smem, up, (size_t)total_bins, use_graph != 0);
         ++w.n_runs;
         if (cudaStreamSynchronize(w.s0) != cudaSuccess) rc = MCRG_EIO;

@@ -222,12 +222,33 @@ __global__ void __launch_bounds__(MAXT, MINB) pool_kernel(const PoolQueue* __res
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ int s_pack;
   __shared__ ChainJob s_job[kPoolMaxGroups];
-  const int n_packs = q->n_packs;
+  // the class of this SM: its share of the SM ids
+  int home = 0;
+  if (threadIdx.x == 0) {
+    unsigned smid, nsmid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+    const int frac = (int)(((unsigned long long)smid << 16) / (nsmid ? nsmid : 1u));
+    for (int k = 1; k < q->n_classes; ++k)
+      if (frac >= q->sm_edge[k]) home = k;
+  }
+  unsigned done_mask = 0;  // classes found empty (thread 0)
   for (;;) {
-    if (threadIdx.x == 0) s_pack = (int)atomicAdd(q->next, 1u);
+    if (threadIdx.x == 0) {
+      int p = -1;
+      for (int j = 0; j < q->n_classes && p < 0; ++j) {
+        const int k = (home + j) % q->n_classes;
+        if ((done_mask >> k) & 1u) continue;
+        const int n_k = q->first[k + 1] - q->first[k];
+        const int i = n_k > 0 ? (int)atomicAdd(q->next + 16 * k, 1u) : n_k;
+        if (i < n_k) p = q->first[k] + i;
+        else done_mask |= 1u << k;
+      }
+      s_pack = p;
+    }
     __syncthreads();
     const int p = s_pack;
-    if (p >= n_packs) break;
+    if (p < 0) break;
     const PoolPack pk = q->packs[p];
     const int g = (int)threadIdx.x / pk.threads, tid = (int)threadIdx.x - g * pk.threads;
     if (g < pk.count) {

@@ -144,12 +144,22 @@ struct PoolPack {
   int32_t stride;
   int32_t pad;
 };
+// The packs are grouped into up to kPoolClasses classes by chain code (byte
+// sweeps, plane sweeps, cluster updates): class k is packs [first[k],
+// first[k+1]).  A CTA serves first the class of its SM (SM id ×
+// n_classes-weighted by class work: sm_edge[k] = first SM fraction, in
+// 1/65536, of class k), then takes from the others when it is empty, so that
+// the CTAs of one SM mostly run one chain code and share its instructions in
+// cache.  next[k * 16] counts the packs of class k handed out.
+constexpr int kPoolClasses = 3;
 struct PoolQueue {
   int32_t n_packs;
-  int32_t pad;
+  int32_t n_classes;
   const PoolPack* packs;
   const ChainJob* jobs;
-  unsigned* next;  // packs handed out so far; zero before the launch
+  unsigned* next;  // per class, 64 bytes apart; zero before the launch
+  int32_t first[kPoolClasses + 1];
+  int32_t sm_edge[kPoolClasses + 1];
 };
 // Served requests (serve_kernel, mcrg_chain.cu): a ring of packs in page-
 // locked host memory that the server's scheduler fills and the persistent
