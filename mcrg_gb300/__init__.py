@@ -424,7 +424,15 @@ def batch_stats(device: int = 0) -> dict:
 
 
 class Server:
-    """Continuous-batching MCRG server (mcrg_server_*)."""
+    """Continuous-batching MCRG server (mcrg_server_*).
+
+    Requests are admitted in arrival order while slots and the HBM budget
+    allow; resident ones run in the device-resident request loop (persistent
+    CTAs draining a ring in page-locked host memory), the rest on worker
+    threads inside their share of the budget's arena.  A result depends only
+    on its request's seed and replica.  Time the shapes you serve with
+    batch_schedule() first to let the loop use the autotuned threads per
+    chain."""
 
     def __init__(self, device: int = 0, slots: int = 256, hbm_budget_bytes: int = 1 << 30, queue_capacity: int = 1 << 16,
                  hbm_workers: int = 0):
