@@ -29,6 +29,7 @@
 #include "mcrg_ops.cuh"
 #include "mcrg_resident_bits.cuh"
 #include "mcrg_resident_cluster.cuh"
+#include "mcrg_small_levels.cuh"
 
 namespace mcrg {
 
@@ -108,6 +109,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
     tab[e] = make_int2(x | (y << 16), out);
     macc[e] = 0;
   }
+  for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
   if (bits && tid < 2) qn[tid] = 0;
   chain_sync(T);
 
@@ -127,69 +129,81 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
   for (int64_t s = 0; s < J.n_eq; ++s) step(t++);
   for (int64_t n = 0; n < J.n_samples; ++n) {
     for (int64_t s = 0; s < J.sweeps_between; ++s) step(t++);
-    // ---- measurement: coupling sums of every level, blocking level by level
+    // ---- measurement.  Levels of side >= 64: the whole chain, sums into S by
+    //      shared-memory atomics (S is zero here), a barrier after each blocking.
+    //      Levels of side <= 32: warp 0 from row words in registers.
     const uint32_t sample = J.n0 + (uint32_t)n;
-    for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += T) S[x] = 0;
-    chain_sync(T);
-    int m = L;
-    for (int l = 0; l <= nl; ++l, m >>= 1) {
+    if (J.sweeps_between == 0) chain_sync(T);  // no step since the last measurement reset S
+    int m = L, l = 0;
+    bool in_regs = false;  // warp 0 holds level l as row words
+    uint32_t row = 0;
+    while (l <= nl && m >= 64) {
       const uint8_t* lev = smem + plan.off[l];
       int a5[5] = {0, 0, 0, 0, 0};
-      if (bits && m >= 64) {
+      if (bits) {
         const uint32_t* P = reinterpret_cast<const uint32_t*>(lev);
         if (C <= 2) resident::couplings_planes<2>(P, m, tid, T, a5);
         else resident::couplings_planes<5>(P, m, tid, T, a5);
-      } else if (m >= 32) {
+      } else {
         if (C <= 2) couplings_vec<4, 2>(lev, m, tid, T, a5);
         else couplings_vec<4>(lev, m, tid, T, a5);
-      } else if (m == 16) {
-        if (C <= 2) couplings_vec<2, 2>(lev, m, tid, T, a5);
-        else couplings_vec<2>(lev, m, tid, T, a5);
+      }
+      if (C <= 2) reduce_into<2>(a5, S + l * MCRG_MAX_COUPLINGS, C);
+      else reduce_into<5>(a5, S + l * MCRG_MAX_COUPLINGS, C);
+      if (l == nl) break;
+      if (bits && m == 64) {  // the blocking into side 32 lands in warp 0's registers
+        if (tid < 32) row = small::block_planes_row(reinterpret_cast<const uint32_t*>(lev), key, rep, l + 1, sample, tid);
+        in_regs = true;
       } else {
-        couplings_scalar(lev, m, tid, T, a5);
-      }
-      reduce_into(a5, S + l * MCRG_MAX_COUPLINGS, C);
-      if (l < nl) {
         uint8_t* nxt = smem + plan.off[l + 1];
-        if (bits && m >= 64)
-          resident::block_planes(reinterpret_cast<const uint32_t*>(lev), m, nxt, key, rep, l + 1, sample, tid, T);
-        else if (m >= 32) block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
-        else block_scalar(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
+        if (bits) resident::block_planes(reinterpret_cast<const uint32_t*>(lev), m, nxt, key, rep, l + 1, sample, tid, T);
+        else block_vec(lev, m, nxt, nullptr, key, rep, l + 1, sample, tid, T);
+        chain_sync(T);
       }
-      chain_sync(T);
+      ++l;
+      m >>= 1;
     }
-    // ---- moment products (each entry owned by one thread)
-    for (int e = tid; e < E; e += T) {
-      const int2 te = tab[e];
-      const long long xv = S[te.x & 0xFFFF];
-      const int yi = (te.x >> 16) & 0xFFFF;
-      macc[e] += yi == 0xFFFF ? xv : xv * (long long)S[yi];
+    if (l <= nl && m <= 32 && tid < 32) {
+      if (!in_regs) row = tid < m ? small::level_row(smem + plan.off[l], m, tid) : 0u;
+      if (C <= 2) small::levels<2>(row, m, l, nl, C, key, rep, sample, S);
+      else small::levels<5>(row, m, l, nl, C, key, rep, sample, S);
     }
-    // ---- bin boundary: flush and restart the sums
-    const bool last = n == J.n_samples - 1;
-    if ((n + 1) % J.bin_size == 0 || last) {
-      mcrg_moments* out = J.bins + n / J.bin_size;
-      for (int e = tid; e < E; e += T) {
-        const int o = tab[e].y, kind = o >> 16, idx = o & 0xFFFF;
-        const long long v = macc[e];
-        if (kind == 0) {
-          out->S[idx] = v;
-        } else {
-          mcrg_i128 w;
-          w.lo = (uint64_t)v;
-          w.hi = v >> 63;
-          if (kind == 1) out->SbS[idx] = w;
-          else out->SbSb[idx] = w;
+    chain_sync(T);  // every sum in S; nobody reads this sample's levels any more
+    // ---- moment products, bin flush and the reset of S: warp 0, each entry
+    //      owned by one lane (the other warps go on with the next steps)
+    if (tid < 32) {
+      for (int e = tid; e < E; e += 32) {
+        const int2 te = tab[e];
+        const long long xv = S[te.x & 0xFFFF];
+        const int yi = (te.x >> 16) & 0xFFFF;
+        macc[e] += yi == 0xFFFF ? xv : xv * (long long)S[yi];
+      }
+      const bool last = n == J.n_samples - 1;
+      if ((n + 1) % J.bin_size == 0 || last) {
+        mcrg_moments* out = J.bins + n / J.bin_size;
+        for (int e = tid; e < E; e += 32) {
+          const int o = tab[e].y, kind = o >> 16, idx = o & 0xFFFF;
+          const long long v = macc[e];
+          if (kind == 0) {
+            out->S[idx] = v;
+          } else {
+            mcrg_i128 w;
+            w.lo = (uint64_t)v;
+            w.hi = v >> 63;
+            if (kind == 1) out->SbS[idx] = w;
+            else out->SbSb[idx] = w;
+          }
+          macc[e] = 0;
         }
-        macc[e] = 0;
+        if (tid == 0) {
+          out->n_levels = nl;
+          out->n_couplings = C;
+          out->n_samples = last ? (n % J.bin_size) + 1 : J.bin_size;
+        }
       }
-      if (tid == 0) {
-        out->n_levels = nl;
-        out->n_couplings = C;
-        out->n_samples = last ? (n % J.bin_size) + 1 : J.bin_size;
-      }
+      __syncwarp();
+      for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += 32) S[x] = 0;
     }
-    chain_sync(T);
   }
 
   // ---- final configuration back to HBM

@@ -404,10 +404,12 @@ __device__ void block_scalar(const uint8_t* in, int n, uint8_t* out, const uint8
   }
 }
 
+// Warp sums of acc[0 .. NC-1] added into S[c], c < C (NC >= C).
+template <int NC = 5>
 __device__ __forceinline__ void reduce_into(int (&acc)[5], int* S, int C) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int c = 0; c < 5; ++c) {
+  for (int c = 0; c < NC; ++c) {
     const int v = __reduce_add_sync(0xFFFFFFFFu, acc[c]);
     if (lane == 0 && c < C) atomicAdd(&S[c], v);
   }
