@@ -142,7 +142,7 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
       int a5[5] = {0, 0, 0, 0, 0};
       if (bits) {
         const uint32_t* P = reinterpret_cast<const uint32_t*>(lev);
-        if (C <= 2) resident::couplings_planes<2>(P, m, tid, T, a5);
+        if (C <= 2) resident::couplings_planes_c2(P, m, tid, T, a5);
         else resident::couplings_planes<5>(P, m, tid, T, a5);
       } else {
         if (C <= 2) couplings_vec<4, 2>(lev, m, tid, T, a5);

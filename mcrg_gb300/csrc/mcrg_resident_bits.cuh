@@ -91,6 +91,34 @@ __device__ __forceinline__ void couplings_planes(const uint32_t* P, int m, int t
   if (NC > 4) acc[4] += 64 * nw - 2 * a4;
 }
 
+// The first two coupling sums of a plane level (couplings_planes<2>), one
+// item per (row i, word w) covering both colours: the colour with q = 0 (its
+// right and down-right neighbours share its word index) and the colour with
+// q = 1 read the same seven words (rows i and i + 1, words w and one
+// neighbour each), instead of six words per colour.
+__device__ __forceinline__ void couplings_planes_c2(const uint32_t* P, int m, int tid, int T, int (&acc)[5]) {
+  using planes::right_sites;
+  using planes::left_sites;
+  const int wpr = m / 64, lw = log2_words(wpr), words = m * wpr;
+  int a0 = 0, a1 = 0, nw = 0;
+  for (int x = tid; x < words; x += T) {
+    const int i = x >> lw, w = x & (wpr - 1);
+    const int r0 = i * wpr, r1 = ((i + 1) & (m - 1)) * wpr;
+    const uint32_t* Pe = P + (size_t)(i & 1) * words;        // colour i & 1: q = 0
+    const uint32_t* Po = P + (size_t)((i + 1) & 1) * words;  // the other colour: q = 1
+    const uint32_t ce = Pe[r0 + w], co = Po[r0 + w], cen = Pe[r0 + ((w + 1) & (wpr - 1))];
+    const uint32_t de = Pe[r1 + w], dd = Po[r1 + w];
+    // q = 0: down O[i+1][k] = dd, right O[i][k] = co;  q = 1: down de, right O[i][k+1]
+    a0 += __popc(ce ^ dd) + __popc(ce ^ co) + __popc(co ^ de) + __popc(co ^ right_sites(ce, cen));
+    // q = 0: C[i+1][k] = de and C[i+1][k-1];  q = 1: C[i+1][k+1] and C[i+1][k] = dd
+    a1 += __popc(ce ^ de) + __popc(ce ^ left_sites(de, Pe[r1 + ((w - 1) & (wpr - 1))])) +
+          __popc(co ^ right_sites(dd, Po[r1 + ((w + 1) & (wpr - 1))])) + __popc(co ^ dd);
+    ++nw;
+  }
+  acc[0] += 256 * nw - 4 * a0;
+  acc[1] += 256 * nw - 4 * a1;
+}
+
 // b = 2 majority blocking of a plane level of side m >= 64 into level m/2:
 // plane words when m/2 >= 64, split-layout bytes when m == 64.  Block (ib, jb)
 // counts split column jb of rows 2ib, 2ib+1 in both colours (bit pos(jb & 31)
@@ -107,9 +135,8 @@ __device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* 
   if (h >= 64) {
     uint32_t* Q = reinterpret_cast<uint32_t*>(out);
     const int wpr1 = wpr / 2, lw1 = log2_words(wpr1), words1 = h * wpr1;
-    for (int x = tid; x < words1; x += T) {
-      const int ib = x >> lw1, w1 = x & (wpr1 - 1);
-      const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample);
+    // output word x = (ib, w1) from input words 2 w1, 2 w1 + 1 of rows 2 ib, 2 ib + 1
+    auto out_word = [&](int x, int ib, int w1, const uint4& tb) {
       uint32_t res[2];
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
@@ -122,6 +149,20 @@ __device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* 
       const uint32_t z1 = ((res[0] >> 8) & 0x00FF00FFu) | (res[1] & 0xFF00FF00u);  // odd jb
       Q[(size_t)(ib & 1) * words1 + x] = planes::unshuffle(z0);
       Q[(size_t)((ib + 1) & 1) * words1 + x] = planes::unshuffle(z1);
+    };
+    if (wpr1 >= 2) {  // output words 2a, 2a + 1 of a row draw their ties from one block (group a)
+      for (int y = tid; y < words1 / 2; y += T) {
+        const int x = 2 * y, ib = x >> lw1, w1 = x & (wpr1 - 1);
+        const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample);
+        out_word(x, ib, w1, tb);
+        out_word(x + 1, ib, w1 + 1, tb);
+      }
+    } else {
+      for (int x = tid; x < words1; x += T) {
+        const int ib = x >> lw1, w1 = x & (wpr1 - 1);
+        out_word(x, ib, w1,
+                 stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample));
+      }
     }
   } else {  // m == 64: 32 rows of one word per colour -> bytes of side 32 (16 per colour row)
     for (int ib = tid; ib < 32; ib += T) {
