@@ -253,9 +253,15 @@ __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key 
         const uint4 hi = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 4), t);
         r8 = (u4get(hi, (k & 15) >> 2) >> (8 * (k & 3))) & 0xFFu;
       }
-      const uint4 lo = stream_block(key, rep, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
-      const uint32_t u32 = (r8 << 24) | (u4get(lo, k & 3) & 0xFFFFFFu);
-      flip = u32 < a.thr[m];
+      // u32 = r8 << 24 | r24 < thr: the top byte decides unless it ties, and only
+      // then is the P_SWEEP_LO draw needed
+      const uint32_t th = a.thr[m];
+      if (r8 != (th >> 24)) {
+        flip = r8 < (th >> 24);
+      } else {
+        const uint4 lo = stream_block(key, rep, P_SWEEP_LO, (uint32_t)c, (uint32_t)i, (uint32_t)(k >> 2), t);
+        flip = (u4get(lo, k & 3) & 0xFFFFFFu) < (th & 0xFFFFFFu);
+      }
     }
     if (flip) Cc[(size_t)i * half + k] = (uint8_t)(tv ^ 1u);
   }
