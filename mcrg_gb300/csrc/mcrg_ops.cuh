@@ -143,7 +143,7 @@ __device__ __forceinline__ void warp_resolve_resident(uint8_t* lat, int n, int c
     uint32_t bits = om[r];
     if (!bits) continue;
     const int task = base + tid + r * T;
-    const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB;
+    const int i = task >> (__ffs(cpr) - 1), k0 = (task & (cpr - 1)) * CB;
     while (bits) {
       const int p = __ffs(bits) - 1;
       bits &= bits - 1;
@@ -168,7 +168,7 @@ template <int NW>
 __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
                                  const Accept& a, int tid, int T, uint32_t* scratch) {
   constexpr int CB = 4 * NW;  // chunk bytes
-  const int half = n / 2, cpr = half / CB, ntask = n * cpr;
+  const int half = n / 2, cpr = half / CB, ntask = n * cpr, lc = __ffs(cpr) - 1;  // cpr: a power of two
   uint8_t* Cc = lat + (size_t)c * n * half;
   const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
   for (int base = 0; base < ntask; base += 8 * T) {
@@ -178,7 +178,7 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
       const int task = base + tid + r * T;
       om[r] = 0;
       if (task < ntask) {
-        const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB;
+        const int i = task >> lc, k0 = (task & (cpr - 1)) * CB;
         const uint32_t q = (uint32_t)((i + c) & 1);
         uint8_t* tp = Cc + (size_t)i * half + k0;
         const uint8_t* orow = Oc + (size_t)i * half;
@@ -204,7 +204,7 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
         uint32_t bits = om[r];
         if (!bits) continue;
         const int task = base + tid + r * T;
-        const int i = task / cpr, k0 = (task - (task / cpr) * cpr) * CB, q = (i + c) & 1;
+        const int i = task >> lc, k0 = (task & (cpr - 1)) * CB, q = (i + c) & 1;
         const uint8_t* orow = Oc + (size_t)i * half;
         while (bits) {
           const int p = __ffs(bits) - 1;
@@ -226,11 +226,11 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
 // n >= 64 (the layouts of the byte-SWAR and bit-sliced sweeps).
 __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key key, uint32_t rep,
                                     const Accept& a, int tid, int T) {
-  const int half = n / 2;
+  const int half = n / 2, lh = __ffs(half) - 1;  // half is a power of two
   uint8_t* Cc = lat + (size_t)c * n * half;
   const uint8_t* Oc = lat + (size_t)(1 - c) * n * half;
   for (int s = tid; s < n * half; s += T) {
-    const int i = s / half, k = s % half, q = (i + c) & 1;
+    const int i = s >> lh, k = s & (half - 1), q = (i + c) & 1;
     const uint32_t tv = Cc[(size_t)i * half + k];
     const uint32_t m = (Oc[(size_t)((i - 1) & (n - 1)) * half + k] != tv) +
                        (Oc[(size_t)((i + 1) & (n - 1)) * half + k] != tv) +
@@ -276,9 +276,9 @@ __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key 
 template <int NW, int NC = 5>
 __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&acc)[5]) {
   constexpr int CB = 4 * NW;
-  const int half = n / 2, cpr = half / CB;
+  const int half = n / 2, cpr = half / CB, lc = __ffs(cpr) - 1, lnc = __ffs(n * cpr) - 1;  // powers of two
   for (int task = tid; task < 2 * n * cpr; task += T) {
-    const int c = task / (n * cpr), rem = task % (n * cpr), i = rem / cpr, k0 = (rem % cpr) * CB;
+    const int c = task >> lnc, rem = task & (n * cpr - 1), i = rem >> lc, k0 = (rem & (cpr - 1)) * CB;
     const uint32_t q = (uint32_t)((i + c) & 1);
     const uint8_t* C = lev + (size_t)c * n * half;
     const uint8_t* O = lev + (size_t)(1 - c) * n * half;
@@ -360,8 +360,9 @@ __device__ void block_vec(const uint8_t* in, int n, uint8_t* out, const uint8_t*
   const int half = n / 2, hn = n / 2, ohalf = hn / 2, cpr = hn / 16;
   const uint8_t* B = in;
   const uint8_t* W = in + (size_t)n * half;
+  const int lc = __ffs(cpr) - 1;  // cpr: a power of two
   for (int task = tid; task < hn * cpr; task += T) {
-    const int ib = task / cpr, jb0 = (task % cpr) * 16;
+    const int ib = task >> lc, jb0 = (task & (cpr - 1)) * 16;
     uint32_t b0[4], w0[4], b1[4], w1[4];
     load_words4(B + (size_t)(2 * ib) * half + jb0, b0);
     load_words4(W + (size_t)(2 * ib) * half + jb0, w0);
