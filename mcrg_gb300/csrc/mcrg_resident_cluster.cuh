@@ -132,14 +132,15 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
     uint32_t* hb = reinterpret_cast<uint32_t*>(work + hb_off(n));
     uint32_t* vb = reinterpret_cast<uint32_t*>(work + vb_off(n));
     const int segs = L / 32, units = L * segs, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
+    const int ls = __ffs(segs) - 1;  // L is a power of two: divisions by segs are shifts
     // runs: unit u = row u / segs, columns 32 (u % segs) .. +31; two units per pass,
     // lane l draws pair l & 15 of unit 2v + (l >> 4)
     for (int v = warp; v < units / 2; v += nw) {
-      const int ud = 2 * v + (lane >> 4), di = ud / segs, dj = (ud - di * segs) * 32;
+      const int ud = 2 * v + (lane >> 4), di = ud >> ls, dj = (ud & (segs - 1)) * 32;
       const uint4 R = stream_block(key, rep, P_BOND, 0u, (uint32_t)di, (uint32_t)((dj >> 1) + (lane & 15)), t);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int u = 2 * v + h, i = u / segs, j0 = (u - i * segs) * 32, src = h * 16 + (lane >> 1);
+        const int u = 2 * v + h, i = u >> ls, j0 = (u & (segs - 1)) * 32, src = h * 16 + (lane >> 1);
         const uint32_t wx = __shfl_sync(0xFFFFFFFFu, R.x, src), wy = __shfl_sync(0xFFFFFFFFu, R.y, src);
         const uint32_t wz = __shfl_sync(0xFFFFFFFFu, R.z, src), ww = __shfl_sync(0xFFFFFFFFu, R.w, src);
         const uint32_t ur = (lane & 1) ? wz : wx, udn = (lane & 1) ? ww : wy;
@@ -159,7 +160,7 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
     }
     chain_sync(T);
     for (int u = warp; u < units; u += nw) {
-      const int i = u / segs, sg = u - i * segs, j0 = sg * 32, in = (i + 1) & m;
+      const int i = u >> ls, sg = u & (segs - 1), j0 = sg * 32, in = (i + 1) & m;
       const uint32_t vv = vb[u], hr = hb[u], hn = hb[in * segs + sg];
       const uint32_t dup = (vv & hr & hn) << 1;  // column c-1 already joins the same two runs
       if (((vv & ~dup) >> lane) & 1u) unite16<true>(lab, i * L + j0 + lane, in * L + j0 + lane);
@@ -170,7 +171,7 @@ __device__ void update(const Level& lv, int L, uint8_t* work, Key key, uint32_t 
     chain_sync(T);
     // open bonds of site pairs (i, j0), (i, j0 + 1): one Philox block each
     for (int y = tid; y < n / 2; y += T) {
-      const int i = y / half, j0 = 2 * (y - i * half), id = (i + 1) & m, x0 = i * L + j0;
+      const int i = y >> (__ffs(half) - 1), j0 = 2 * (y & (half - 1)), id = (i + 1) & m, x0 = i * L + j0;
       const uint4 r = stream_block(key, rep, P_BOND, 0u, (uint32_t)i, (uint32_t)(j0 >> 1), t);
       const uint32_t s0 = lv.spin(i, j0), s1 = lv.spin(i, j0 + 1);
       if (r.x < tb && s1 == s0) unite16(lab, x0, x0 + 1);
@@ -212,7 +213,7 @@ __device__ __forceinline__ void update_bytes(uint8_t* lat, int L, uint8_t* work,
   const bool wolff = kind == MCRG_UPDATE_WOLFF;
   for (int x = tid; x < L * L; x += T)
     if (flips(work, L, x, wolff)) {
-      const int i = x / L, j = x - i * L;
+      const int i = x >> (__ffs(L) - 1), j = x & (L - 1);
       lat[(size_t)((i + j) & 1) * L * h + (size_t)i * h + (j >> 1)] ^= 1u;
     }
   chain_sync(T);
@@ -225,7 +226,7 @@ __device__ __forceinline__ void update_planes(uint32_t* pl, int L, uint8_t* work
   const int wpr = L / 64, words = L * wpr;
   const bool wolff = kind == MCRG_UPDATE_WOLFF;
   for (int x = tid; x < 2 * words; x += T) {
-    const int c = x >= words, r = x - c * words, i = r / wpr, w = r - i * wpr, q = (i + c) & 1;
+    const int c = x >= words, r = x - c * words, i = r >> (__ffs(wpr) - 1), w = r & (wpr - 1), q = (i + c) & 1;
     uint32_t mask = 0;
     for (int p = 0; p < 32; ++p)
       if (flips(work, L, i * L + 2 * (32 * w + p) + q, wolff)) mask |= 1u << planes::plane_pos(p);
