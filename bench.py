@@ -407,7 +407,7 @@ def batched_cfg(args, D: Dist) -> dict:
             "equal_error": "same seeds: batched and plain runs give bit-identical moment sums, so identical "
                            "T-eigenvalue estimates and error bars (checked on the timed plain requests)",
             "threads_per_chain": sched, "graph_builds": st["graph_builds"], "launches": st["launches"],
-            "roofline": {"bound": "sm_issue", "kernel": "pool_kernel<256,3>",
+            "roofline": {"bound": "sm_issue", "kernel": "pool_kernel<256,2>",
                          "issue_active_frac": profiled("issue_active_frac", "pool_kernel_batched"),
                          "source": "ncu, profiles/pool_kernel_batched.md (200-sweep batch of the same mix)"},
             "clocks": clocks,

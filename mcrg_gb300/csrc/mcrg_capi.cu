@@ -90,11 +90,11 @@ __device__ __forceinline__ uint32_t pm1_to_01(uint32_t x, uint32_t& bad) {
 
 __global__ void nat_to_split_vec_kernel(const int8_t* __restrict__ nat, int N, uint8_t* __restrict__ split,
                                         int* __restrict__ bad) {
-  const int half = N / 2, per_row = N / 32;
+  const int half = N / 2, per_row = N / 32, lp = __ffs(per_row) - 1;  // N: a power of two
   uint32_t b = 0;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < (long long)N * per_row;
        q += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(q / per_row), j0 = (int)(q - (long long)i * per_row) * 32;
+    const int i = (int)(q >> lp), j0 = (int)(q & (per_row - 1)) * 32;
     const uint4* src = reinterpret_cast<const uint4*>(nat + (size_t)i * N + j0);
     const uint4 a = src[0], c = src[1];
     const uint32_t w[8] = {pm1_to_01(a.x, b), pm1_to_01(a.y, b), pm1_to_01(a.z, b), pm1_to_01(a.w, b),
@@ -111,10 +111,10 @@ __global__ void nat_to_split_vec_kernel(const int8_t* __restrict__ nat, int N, u
 }
 
 __global__ void split_to_nat_vec_kernel(const uint8_t* __restrict__ split, int N, int8_t* __restrict__ nat) {
-  const int half = N / 2, per_row = N / 32;
+  const int half = N / 2, per_row = N / 32, lp = __ffs(per_row) - 1;  // N: a power of two
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < (long long)N * per_row;
        q += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(q / per_row), j0 = (int)(q - (long long)i * per_row) * 32, ce = i & 1;
+    const int i = (int)(q >> lp), j0 = (int)(q & (per_row - 1)) * 32, ce = i & 1;
     const uint4 e = *reinterpret_cast<const uint4*>(split + (size_t)ce * N * half + (size_t)i * half + (j0 >> 1));
     const uint4 o = *reinterpret_cast<const uint4*>(split + (size_t)(1 - ce) * N * half + (size_t)i * half + (j0 >> 1));
     const uint32_t E[4] = {e.x, e.y, e.z, e.w}, O[4] = {o.x, o.y, o.z, o.w};

@@ -411,9 +411,11 @@ cudaError_t serve_prepare(int smem, int* blocks_per_sm) {
 
 // The 512-wide instantiation runs one CTA per SM: held to 64 registers for
 // two, the chain code spills (measured 6-7 % slower on batches of cluster
-// chains).
+// chains).  The 256-wide one runs two per SM: the plane sweep's two words per
+// thread and step need ~120 registers (held to 80 for three CTAs it spilled,
+// and three CTAs of the one-word sweep were 3 % slower on the batched mix).
 const void* pool_kernel_fn(int cta_threads) {
-  return cta_threads > 256 ? (const void*)pool_kernel<512, 1> : (const void*)pool_kernel<256, 3>;
+  return cta_threads > 256 ? (const void*)pool_kernel<512, 1> : (const void*)pool_kernel<256, 2>;
 }
 
 cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm) {
@@ -430,7 +432,7 @@ cudaError_t pool_prepare(int cta_threads, int smem, int* blocks_per_sm) {
     configured[wide].fetch_or(bit, std::memory_order_release);
   }
   return wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<512, 1>, cta_threads, smem)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<256, 3>, cta_threads, smem);
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pool_kernel<256, 2>, cta_threads, smem);
 }
 
 cudaError_t launch_block_once(const uint8_t* d_in, int N, uint8_t* d_out, const uint8_t* d_tie_nat, Key key,

@@ -231,19 +231,21 @@ __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_
       to[p] = 0u - ((T1 >> (7 - p)) & 1u);
     }
   }
-  for (int r = tid; r < words; r += T) {
-    const int i = r >> lw, w = r & (wpr - 1);
+  // two words per thread and step (r and r + T): two independent Philox and
+  // decision chains in flight per thread
+  auto neighbours = [&](int r, int& i, int& w, uint32_t& tv, uint32_t& u, uint32_t& d, uint32_t& mid,
+                        uint32_t& side) {
+    i = r >> lw;
+    w = r & (wpr - 1);
     const uint32_t* orow = Oc + (size_t)i * wpr;
-    const uint32_t tv = Cc[r];
-    const uint32_t u = Oc[(size_t)((i - 1) & (L - 1)) * wpr + w];
-    const uint32_t d = Oc[(size_t)((i + 1) & (L - 1)) * wpr + w];
-    const uint32_t mid = orow[w];
-    const uint32_t side = ((i + c) & 1) ? planes::right_sites(mid, orow[(w + 1) & (wpr - 1)])
-                                        : planes::left_sites(mid, orow[(w - 1) & (wpr - 1)]);
-    const uint4 A = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w), t);
-    const uint4 B = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(2 * w + 1), t);
-    uint32_t open, zero;
-    uint32_t nt = planes::decide(tv, u, d, mid, side, A, B, tz, to, open, zero);
+    tv = Cc[r];
+    u = Oc[(size_t)((i - 1) & (L - 1)) * wpr + w];
+    d = Oc[(size_t)((i + 1) & (L - 1)) * wpr + w];
+    mid = orow[w];
+    side = ((i + c) & 1) ? planes::right_sites(mid, orow[(w + 1) & (wpr - 1)])
+                         : planes::left_sites(mid, orow[(w - 1) & (wpr - 1)]);
+  };
+  auto finish = [&](int r, int i, int w, uint32_t nt, uint32_t open, uint32_t zero) {
     if (open) {
       const int slot = atomicAdd(&qn[c], 1);
       if (slot < cap)
@@ -252,6 +254,23 @@ __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_
         nt ^= open_flips(key, rep, a, c, i, w, open, zero, t);
     }
     Cc[r] = nt;
+  };
+  for (int r = tid; r < words; r += 2 * T) {
+    const bool two = r + T < words;
+    const int r2 = two ? r + T : r;
+    int i1, w1, i2, w2;
+    uint32_t tv1, u1, d1, m1, s1, tv2, u2, d2, m2, s2;
+    neighbours(r, i1, w1, tv1, u1, d1, m1, s1);
+    neighbours(r2, i2, w2, tv2, u2, d2, m2, s2);
+    const uint4 A1 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i1, (uint32_t)(2 * w1), t);
+    const uint4 A2 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i2, (uint32_t)(2 * w2), t);
+    const uint4 B1 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i1, (uint32_t)(2 * w1 + 1), t);
+    const uint4 B2 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i2, (uint32_t)(2 * w2 + 1), t);
+    uint32_t o1, z1, o2, z2;
+    const uint32_t n1 = planes::decide(tv1, u1, d1, m1, s1, A1, B1, tz, to, o1, z1);
+    const uint32_t n2 = planes::decide(tv2, u2, d2, m2, s2, A2, B2, tz, to, o2, z2);
+    finish(r, i1, w1, n1, o1, z1);
+    if (two) finish(r2, i2, w2, n2, o2, z2);
   }
   chain_sync(T);
   const int nq = min(qn[c], cap);
