@@ -255,9 +255,9 @@ __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_
     }
     Cc[r] = nt;
   };
-  for (int r = tid; r < words; r += 2 * T) {
-    const bool two = r + T < words;
-    const int r2 = two ? r + T : r;
+  int r = tid;
+  for (; r + T < words; r += 2 * T) {
+    const int r2 = r + T;
     int i1, w1, i2, w2;
     uint32_t tv1, u1, d1, m1, s1, tv2, u2, d2, m2, s2;
     neighbours(r, i1, w1, tv1, u1, d1, m1, s1);
@@ -270,7 +270,17 @@ __device__ __forceinline__ void sweep_colour(uint32_t* pl, int L, int c, uint32_
     const uint32_t n1 = planes::decide(tv1, u1, d1, m1, s1, A1, B1, tz, to, o1, z1);
     const uint32_t n2 = planes::decide(tv2, u2, d2, m2, s2, A2, B2, tz, to, o2, z2);
     finish(r, i1, w1, n1, o1, z1);
-    if (two) finish(r2, i2, w2, n2, o2, z2);
+    finish(r2, i2, w2, n2, o2, z2);
+  }
+  if (r < words) {  // one word left for this thread (words per thread odd, e.g. one when T = words)
+    int i1, w1;
+    uint32_t tv1, u1, d1, m1, s1;
+    neighbours(r, i1, w1, tv1, u1, d1, m1, s1);
+    const uint4 A1 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i1, (uint32_t)(2 * w1), t);
+    const uint4 B1 = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i1, (uint32_t)(2 * w1 + 1), t);
+    uint32_t o1, z1;
+    const uint32_t n1 = planes::decide(tv1, u1, d1, m1, s1, A1, B1, tz, to, o1, z1);
+    finish(r, i1, w1, n1, o1, z1);
   }
   chain_sync(T);
   const int nq = min(qn[c], cap);
