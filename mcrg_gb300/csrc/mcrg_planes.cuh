@@ -50,9 +50,31 @@ __device__ __forceinline__ uint32_t unshuffle(uint32_t x) {
   return x;
 }
 
+// Swap of index bits i < j of every bit position (delta d = 2^j - 2^i, m =
+// the positions whose index has bit i set and bit j clear).
+template <int D, uint32_t M>
+__device__ __forceinline__ uint32_t index_swap(uint32_t x) {
+  const uint32_t t = (x ^ (x >> D)) & M;
+  return x ^ t ^ (t << D);
+}
+
 // Natural bit order (bit p = site p) -> plane order (bit pos(p)): pos(p)
-// rotates the index of p right by two.
-__device__ __forceinline__ uint32_t nat_to_plane(uint32_t v) { return unshuffle(unshuffle(v)); }
+// rotates the 5-bit index of p right by two, (a2 a1 a0 b1 b0) -> (b1 b0 a2
+// a1 a0), four index-bit swaps: (1,4), (0,3), (0,2), (1,2).
+__device__ __forceinline__ uint32_t nat_to_plane(uint32_t v) {
+  v = index_swap<14, 0x0000CCCCu>(v);
+  v = index_swap<7, 0x00AA00AAu>(v);
+  v = index_swap<3, 0x0A0A0A0Au>(v);
+  return index_swap<2, 0x0C0C0C0Cu>(v);
+}
+
+// Plane order -> natural order: the same swaps in reverse.
+__device__ __forceinline__ uint32_t plane_to_nat(uint32_t v) {
+  v = index_swap<2, 0x0C0C0C0Cu>(v);
+  v = index_swap<3, 0x0A0A0A0Au>(v);
+  v = index_swap<7, 0x00AA00AAu>(v);
+  return index_swap<14, 0x0000CCCCu>(v);
+}
 
 // Bit-sliced count of four words: ge3 = at least three bits set, eq2 = exactly two.
 __device__ __forceinline__ void majority4(uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t& ge3,

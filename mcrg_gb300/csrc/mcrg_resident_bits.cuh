@@ -92,28 +92,39 @@ __device__ __forceinline__ void couplings_planes(const uint32_t* P, int m, int t
 }
 
 // The first two coupling sums of a plane level (couplings_planes<2>), one
-// item per (row i, word w) covering both colours: the colour with q = 0 (its
-// right and down-right neighbours share its word index) and the colour with
-// q = 1 read the same seven words (rows i and i + 1, words w and one
-// neighbour each), instead of six words per colour.
+// item per row i covering both colours: the colour with q = 0 (its right and
+// down-right neighbours share its word index) and the colour with q = 1 read
+// the words of rows i and i + 1 once each, walking the row's words with the
+// neighbours of word w carried over from word w - 1 (four loads per pair of
+// words instead of six per word).
 __device__ __forceinline__ void couplings_planes_c2(const uint32_t* P, int m, int tid, int T, int (&acc)[5]) {
   using planes::right_sites;
   using planes::left_sites;
-  const int wpr = m / 64, lw = log2_words(wpr), words = m * wpr;
+  const int wpr = m / 64, words = m * wpr;
   int a0 = 0, a1 = 0, nw = 0;
-  for (int x = tid; x < words; x += T) {
-    const int i = x >> lw, w = x & (wpr - 1);
-    const int r0 = i * wpr, r1 = ((i + 1) & (m - 1)) * wpr;
-    const uint32_t* Pe = P + (size_t)(i & 1) * words;        // colour i & 1: q = 0
-    const uint32_t* Po = P + (size_t)((i + 1) & 1) * words;  // the other colour: q = 1
-    const uint32_t ce = Pe[r0 + w], co = Po[r0 + w], cen = Pe[r0 + ((w + 1) & (wpr - 1))];
-    const uint32_t de = Pe[r1 + w], dd = Po[r1 + w];
-    // q = 0: down O[i+1][k] = dd, right O[i][k] = co;  q = 1: down de, right O[i][k+1]
-    a0 += __popc(ce ^ dd) + __popc(ce ^ co) + __popc(co ^ de) + __popc(co ^ right_sites(ce, cen));
-    // q = 0: C[i+1][k] = de and C[i+1][k-1];  q = 1: C[i+1][k+1] and C[i+1][k] = dd
-    a1 += __popc(ce ^ de) + __popc(ce ^ left_sites(de, Pe[r1 + ((w - 1) & (wpr - 1))])) +
-          __popc(co ^ right_sites(dd, Po[r1 + ((w + 1) & (wpr - 1))])) + __popc(co ^ dd);
-    ++nw;
+  for (int i = tid; i < m; i += T) {
+    const int i1 = (i + 1) & (m - 1);
+    const uint32_t* Ce = P + (size_t)(i & 1) * words + (size_t)i * wpr;         // row i, colour i & 1: q = 0
+    const uint32_t* Co = P + (size_t)((i + 1) & 1) * words + (size_t)i * wpr;   // row i, the other colour: q = 1
+    const uint32_t* De = P + (size_t)(i & 1) * words + (size_t)i1 * wpr;        // row i + 1, colour i & 1
+    const uint32_t* Dd = P + (size_t)((i + 1) & 1) * words + (size_t)i1 * wpr;  // row i + 1, the other colour
+    const uint32_t ce0 = Ce[0], dd0 = Dd[0];
+    uint32_t ce = ce0, de = De[0], dd = dd0, dep = De[wpr - 1];
+    for (int w = 0; w < wpr; ++w) {
+      const bool more = w + 1 < wpr;
+      const uint32_t co = Co[w];
+      const uint32_t cen = more ? Ce[w + 1] : ce0, ddn = more ? Dd[w + 1] : dd0;
+      // q = 0: down O[i+1][k] = dd, right O[i][k] = co;  q = 1: down de, right O[i][k+1]
+      a0 += __popc(ce ^ dd) + __popc(ce ^ co) + __popc(co ^ de) + __popc(co ^ right_sites(ce, cen));
+      // q = 0: C[i+1][k] = de and C[i+1][k-1];  q = 1: C[i+1][k+1] and C[i+1][k] = dd
+      a1 += __popc(ce ^ de) + __popc(ce ^ left_sites(de, dep)) + __popc(co ^ right_sites(dd, ddn)) +
+            __popc(co ^ dd);
+      dep = de;
+      de = more ? De[w + 1] : de;
+      ce = cen;
+      dd = ddn;
+    }
+    nw += wpr;
   }
   acc[0] += 256 * nw - 4 * a0;
   acc[1] += 256 * nw - 4 * a1;

@@ -71,15 +71,14 @@ __device__ __forceinline__ uint32_t level_row(const uint8_t* lev, int m, int i) 
 
 // Row ib (= lane, 0..31) of the blocking of a plane level of side 64 into side
 // 32, the rule of resident::block_planes: bit pos(jb) of the majority word is
-// block (ib, jb); plane order back to natural order is the index rotation
-// left by two (shuffle_bits twice).
+// block (ib, jb), brought back to natural order by planes::plane_to_nat.
 __device__ __forceinline__ uint32_t block_planes_row(const uint32_t* P, Key key, uint32_t rep, int level_out,
                                                      uint32_t sample, int ib) {
   const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, 0u, sample);
   uint32_t ge3, eq2;
   planes::majority4(P[2 * ib], P[64 + 2 * ib], P[2 * ib + 1], P[64 + 2 * ib + 1], ge3, eq2);
   const uint32_t res = ge3 | (eq2 & planes::nat_to_plane(tb.x));
-  return shuffle_bits(shuffle_bits(res));
+  return planes::plane_to_nat(res);
 }
 
 // Levels l .. nl of side m, m/2, ... (m <= 32) from `row` (lane i: row i of
