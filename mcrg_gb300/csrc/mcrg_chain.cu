@@ -126,6 +126,8 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
     }
   };
   uint32_t t = J.t0;
+  int64_t bin_fill = 0;           // samples in the current bin (warp 0)
+  mcrg_moments* bin_out = J.bins;  // the current bin (warp 0)
   for (int64_t s = 0; s < J.n_eq; ++s) step(t++);
   for (int64_t n = 0; n < J.n_samples; ++n) {
     for (int64_t s = 0; s < J.sweeps_between; ++s) step(t++);
@@ -179,8 +181,8 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
         macc[e] += yi == 0xFFFF ? xv : xv * (long long)S[yi];
       }
       const bool last = n == J.n_samples - 1;
-      if ((n + 1) % J.bin_size == 0 || last) {
-        mcrg_moments* out = J.bins + n / J.bin_size;
+      if (++bin_fill == J.bin_size || last) {  // (a running count: no 64-bit division per sample)
+        mcrg_moments* out = bin_out++;
         for (int e = tid; e < E; e += 32) {
           const int o = tab[e].y, kind = o >> 16, idx = o & 0xFFFF;
           const long long v = macc[e];
@@ -198,8 +200,9 @@ __device__ __forceinline__ void run_chain(const ChainJob& J, uint8_t* smem, int 
         if (tid == 0) {
           out->n_levels = nl;
           out->n_couplings = C;
-          out->n_samples = last ? (n % J.bin_size) + 1 : J.bin_size;
+          out->n_samples = bin_fill;
         }
+        bin_fill = 0;
       }
       __syncwarp();
       for (int x = tid; x < (MCRG_MAX_LEVELS + 1) * MCRG_MAX_COUPLINGS; x += 32) S[x] = 0;
