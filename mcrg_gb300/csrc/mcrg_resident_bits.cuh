@@ -96,11 +96,15 @@ __device__ __forceinline__ void couplings_planes(const uint32_t* P, int m, int t
 // down-right neighbours share its word index) and the colour with q = 1 read
 // the words of rows i and i + 1 once each, walking the row's words with the
 // neighbours of word w carried over from word w - 1 (four loads per pair of
-// words instead of six per word).
+// words instead of six per word).  Row i starts its walk at word
+// (i / (32 / wpr)) mod wpr, so that the lanes of a warp, one row each, read
+// 32 different shared-memory banks at every step (rows 32 / wpr apart share
+// a bank set).
 __device__ __forceinline__ void couplings_planes_c2(const uint32_t* P, int m, int tid, int T, int (&acc)[5]) {
   using planes::right_sites;
   using planes::left_sites;
-  const int wpr = m / 64, words = m * wpr;
+  const int wpr = m / 64, words = m * wpr, lw = log2_words(wpr);
+  const int lr = lw >= 5 ? 0 : 5 - lw;  // log2 of the rows that share a bank set
   int a0 = 0, a1 = 0, nw = 0;
   for (int i = tid; i < m; i += T) {
     const int i1 = (i + 1) & (m - 1);
@@ -108,19 +112,21 @@ __device__ __forceinline__ void couplings_planes_c2(const uint32_t* P, int m, in
     const uint32_t* Co = P + (size_t)((i + 1) & 1) * words + (size_t)i * wpr;   // row i, the other colour: q = 1
     const uint32_t* De = P + (size_t)(i & 1) * words + (size_t)i1 * wpr;        // row i + 1, colour i & 1
     const uint32_t* Dd = P + (size_t)((i + 1) & 1) * words + (size_t)i1 * wpr;  // row i + 1, the other colour
-    const uint32_t ce0 = Ce[0], dd0 = Dd[0];
-    uint32_t ce = ce0, de = De[0], dd = dd0, dep = De[wpr - 1];
-    for (int w = 0; w < wpr; ++w) {
-      const bool more = w + 1 < wpr;
+    const int w0 = (i >> lr) & (wpr - 1);
+    const uint32_t ce0 = Ce[w0], dd0 = Dd[w0];
+    uint32_t ce = ce0, de = De[w0], dd = dd0, dep = De[(w0 - 1) & (wpr - 1)];
+    for (int k = 0; k < wpr; ++k) {
+      const int w = (w0 + k) & (wpr - 1), wn = (w + 1) & (wpr - 1);
+      const bool more = k + 1 < wpr;
       const uint32_t co = Co[w];
-      const uint32_t cen = more ? Ce[w + 1] : ce0, ddn = more ? Dd[w + 1] : dd0;
+      const uint32_t cen = more ? Ce[wn] : ce0, ddn = more ? Dd[wn] : dd0;
       // q = 0: down O[i+1][k] = dd, right O[i][k] = co;  q = 1: down de, right O[i][k+1]
       a0 += __popc(ce ^ dd) + __popc(ce ^ co) + __popc(co ^ de) + __popc(co ^ right_sites(ce, cen));
       // q = 0: C[i+1][k] = de and C[i+1][k-1];  q = 1: C[i+1][k+1] and C[i+1][k] = dd
       a1 += __popc(ce ^ de) + __popc(ce ^ left_sites(de, dep)) + __popc(co ^ right_sites(dd, ddn)) +
             __popc(co ^ dd);
       dep = de;
-      de = more ? De[w + 1] : de;
+      de = more ? De[wn] : de;
       ce = cen;
       dd = ddn;
     }
@@ -146,33 +152,44 @@ __device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* 
   if (h >= 64) {
     uint32_t* Q = reinterpret_cast<uint32_t*>(out);
     const int wpr1 = wpr / 2, lw1 = log2_words(wpr1), words1 = h * wpr1;
-    // output word x = (ib, w1) from input words 2 w1, 2 w1 + 1 of rows 2 ib, 2 ib + 1
-    auto out_word = [&](int x, int ib, int w1, const uint4& tb) {
-      uint32_t res[2];
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int w = 2 * w1 + hh, ra = 2 * ib * wpr + w, rb = ra + wpr;
-        uint32_t ge3, eq2;
-        planes::majority4(P0[ra], P1[ra], P0[rb], P1[rb], ge3, eq2);
-        res[hh] = ge3 | (eq2 & planes::nat_to_plane(u4get(tb, w & 3)));
-      }
-      const uint32_t z0 = (res[0] & 0x00FF00FFu) | ((res[1] & 0x00FF00FFu) << 8);  // even jb
-      const uint32_t z1 = ((res[0] >> 8) & 0x00FF00FFu) | (res[1] & 0xFF00FF00u);  // odd jb
-      Q[(size_t)(ib & 1) * words1 + x] = planes::unshuffle(z0);
-      Q[(size_t)((ib + 1) & 1) * words1 + x] = planes::unshuffle(z1);
+    // input word w of rows 2 ib, 2 ib + 1 (both colours) -> its blocks in plane order; t: the
+    // tie word of w (natural order)
+    auto block_word = [](uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t t) {
+      uint32_t ge3, eq2;
+      planes::majority4(a0, a1, b0, b1, ge3, eq2);
+      return ge3 | (eq2 & planes::nat_to_plane(t));
     };
-    if (wpr1 >= 2) {  // output words 2a, 2a + 1 of a row draw their ties from one block (group a)
+    // output word x of both colours from the blocks of input words 2 w1, 2 w1 + 1
+    auto out_word = [](uint32_t r0, uint32_t r1, uint32_t& even, uint32_t& odd) {
+      even = planes::unshuffle((r0 & 0x00FF00FFu) | ((r1 & 0x00FF00FFu) << 8));  // even jb
+      odd = planes::unshuffle(((r0 >> 8) & 0x00FF00FFu) | (r1 & 0xFF00FF00u));  // odd jb
+    };
+    if (wpr1 >= 2) {
+      // item y: output words 2y, 2y + 1 of row ib from input words 4a .. 4a + 3 (a = group of the
+      // tie block), read as one 16-byte vector per row and colour; consecutive lanes take
+      // consecutive groups, so a quarter warp's vectors fall on at most two bank sets
       for (int y = tid; y < words1 / 2; y += T) {
-        const int x = 2 * y, ib = x >> lw1, w1 = x & (wpr1 - 1);
+        const int x = 2 * y, ib = x >> lw1, w1 = x & (wpr1 - 1), w = 2 * w1;
         const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample);
-        out_word(x, ib, w1, tb);
-        out_word(x + 1, ib, w1 + 1, tb);
+        const size_t ra = (size_t)2 * ib * wpr + w, rb = ra + wpr;
+        const uint4 a0 = *reinterpret_cast<const uint4*>(P0 + ra), a1 = *reinterpret_cast<const uint4*>(P1 + ra);
+        const uint4 b0 = *reinterpret_cast<const uint4*>(P0 + rb), b1 = *reinterpret_cast<const uint4*>(P1 + rb);
+        uint32_t e0, o0, e1, o1;
+        out_word(block_word(a0.x, a1.x, b0.x, b1.x, tb.x), block_word(a0.y, a1.y, b0.y, b1.y, tb.y), e0, o0);
+        out_word(block_word(a0.z, a1.z, b0.z, b1.z, tb.z), block_word(a0.w, a1.w, b0.w, b1.w, tb.w), e1, o1);
+        *reinterpret_cast<uint2*>(Q + (size_t)(ib & 1) * words1 + x) = make_uint2(e0, e1);
+        *reinterpret_cast<uint2*>(Q + (size_t)((ib + 1) & 1) * words1 + x) = make_uint2(o0, o1);
       }
-    } else {
-      for (int x = tid; x < words1; x += T) {
-        const int ib = x >> lw1, w1 = x & (wpr1 - 1);
-        out_word(x, ib, w1,
-                 stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, (uint32_t)(w1 >> 1), sample));
+    } else {  // m = 128: one output word per row (x = ib) from input words 0, 1 (8-byte vectors)
+      for (int ib = tid; ib < h; ib += T) {
+        const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, 0u, sample);
+        const size_t ra = (size_t)4 * ib, rb = ra + 2;
+        const uint2 a0 = *reinterpret_cast<const uint2*>(P0 + ra), a1 = *reinterpret_cast<const uint2*>(P1 + ra);
+        const uint2 b0 = *reinterpret_cast<const uint2*>(P0 + rb), b1 = *reinterpret_cast<const uint2*>(P1 + rb);
+        uint32_t e, o;
+        out_word(block_word(a0.x, a1.x, b0.x, b1.x, tb.x), block_word(a0.y, a1.y, b0.y, b1.y, tb.y), e, o);
+        Q[(size_t)(ib & 1) * words1 + ib] = e;
+        Q[(size_t)((ib + 1) & 1) * words1 + ib] = o;
       }
     }
   } else {  // m == 64: 32 rows of one word per colour -> bytes of side 32 (16 per colour row)

@@ -75,8 +75,10 @@ __device__ __forceinline__ uint32_t level_row(const uint8_t* lev, int m, int i) 
 __device__ __forceinline__ uint32_t block_planes_row(const uint32_t* P, Key key, uint32_t rep, int level_out,
                                                      uint32_t sample, int ib) {
   const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, 0u, sample);
+  const uint2 c0 = *reinterpret_cast<const uint2*>(P + 2 * ib);       // rows 2ib, 2ib + 1 of colour 0
+  const uint2 c1 = *reinterpret_cast<const uint2*>(P + 64 + 2 * ib);  // and of colour 1
   uint32_t ge3, eq2;
-  planes::majority4(P[2 * ib], P[64 + 2 * ib], P[2 * ib + 1], P[64 + 2 * ib + 1], ge3, eq2);
+  planes::majority4(c0.x, c1.x, c0.y, c1.y, ge3, eq2);
   const uint32_t res = ge3 | (eq2 & planes::nat_to_plane(tb.x));
   return planes::plane_to_nat(res);
 }
