@@ -49,14 +49,21 @@ __device__ __forceinline__ uint32_t shuffle_bits(uint32_t x) {
 // multiply land on distinct bits, bits 24..27 holding the four bytes.
 __device__ __forceinline__ uint32_t nibble4(uint32_t w) { return (w * 0x01020408u) >> 24; }
 
-// n bytes 0/1 (n <= 16) -> bit k = byte k.
+// n bytes 0/1 (n <= 16, p aligned to n) -> bit k = byte k.  Rows of 16 and 8
+// bytes are read as one vector, so that the lanes of a warp (one row each)
+// read consecutive 16 / 8-byte pieces without shared-memory bank conflicts.
 __device__ __forceinline__ uint32_t bytes_to_bits(const uint8_t* p, int n) {
-  uint32_t v = 0;
-  if (n >= 4) {
-    for (int k = 0; k < n; k += 4) v |= nibble4(*reinterpret_cast<const uint32_t*>(p + k)) << k;
-  } else {
-    for (int k = 0; k < n; ++k) v |= (uint32_t)p[k] << k;
+  if (n == 16) {
+    const uint4 v = *reinterpret_cast<const uint4*>(p);
+    return nibble4(v.x) | (nibble4(v.y) << 4) | (nibble4(v.z) << 8) | (nibble4(v.w) << 12);
   }
+  if (n == 8) {
+    const uint2 v = *reinterpret_cast<const uint2*>(p);
+    return nibble4(v.x) | (nibble4(v.y) << 4);
+  }
+  if (n == 4) return nibble4(*reinterpret_cast<const uint32_t*>(p));
+  uint32_t v = 0;
+  for (int k = 0; k < n; ++k) v |= (uint32_t)p[k] << k;
   return v;
 }
 
