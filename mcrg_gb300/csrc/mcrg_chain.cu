@@ -13,7 +13,9 @@
 //
 // Fast acceptance regime, L >= 64: every level of side >= 64 is kept only as
 // bit-plane words; sweeps, coupling sums and blocking of those levels run
-// bit-sliced (mcrg_resident_bits.cuh), the smaller levels as bytes.
+// bit-sliced (mcrg_resident_bits.cuh).  The levels of side <= 32 of every
+// chain are measured by warp 0 from row words in registers
+// (mcrg_small_levels.cuh), without shared memory or barriers per level.
 // Sweep (L <= 32): the 16 sites of a 16-byte chunk of one colour row are updated with
 // byte-SWAR arithmetic from one Philox block (one 8-bit draw per site).  A
 // site whose 8-bit draw equals the top byte of its threshold is left open and

@@ -136,8 +136,9 @@ __device__ __forceinline__ void couplings_planes_c2(const uint32_t* P, int m, in
   acc[1] += 256 * nw - 4 * a1;
 }
 
-// b = 2 majority blocking of a plane level of side m >= 64 into level m/2:
-// plane words when m/2 >= 64, split-layout bytes when m == 64.  Block (ib, jb)
+// b = 2 majority blocking of a plane level of side m >= 128 into the plane
+// level of side m/2 (the blocking of side 64 into 32 lands in one warp's
+// registers: small::block_planes_row).  Block (ib, jb)
 // counts split column jb of rows 2ib, 2ib+1 in both colours (bit pos(jb & 31)
 // of word jb >> 5); a tie takes bit jb & 31 of word (jb & 127) >> 5 of the
 // P_TIE block (level_out, ib, jb >> 7, sample), as block_vec does.  Output
@@ -149,7 +150,7 @@ __device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* 
   const int wpr = m / 64, words = m * wpr, h = m / 2;
   const uint32_t* P0 = P;
   const uint32_t* P1 = P + words;
-  if (h >= 64) {
+  {
     uint32_t* Q = reinterpret_cast<uint32_t*>(out);
     const int wpr1 = wpr / 2, lw1 = log2_words(wpr1), words1 = h * wpr1;
     // input word w of rows 2 ib, 2 ib + 1 (both colours) -> its blocks in plane order; t: the
@@ -190,19 +191,6 @@ __device__ __forceinline__ void block_planes(const uint32_t* P, int m, uint8_t* 
         out_word(block_word(a0.x, a1.x, b0.x, b1.x, tb.x), block_word(a0.y, a1.y, b0.y, b1.y, tb.y), e, o);
         Q[(size_t)(ib & 1) * words1 + ib] = e;
         Q[(size_t)((ib + 1) & 1) * words1 + ib] = o;
-      }
-    }
-  } else {  // m == 64: 32 rows of one word per colour -> bytes of side 32 (16 per colour row)
-    for (int ib = tid; ib < 32; ib += T) {
-      const uint4 tb = stream_block(key, rep, P_TIE, (uint32_t)level_out, (uint32_t)ib, 0u, sample);
-      uint32_t ge3, eq2;
-      planes::majority4(P0[2 * ib], P1[2 * ib], P0[2 * ib + 1], P1[2 * ib + 1], ge3, eq2);
-      const uint32_t res = ge3 | (eq2 & planes::nat_to_plane(tb.x));
-#pragma unroll
-      for (int par = 0; par < 2; ++par) {
-        uint4 a, b;
-        planes::unpack_bytes(planes::unshuffle((res >> (8 * par)) & 0x00FF00FFu), a, b);  // sites 0..15 in a
-        *reinterpret_cast<uint4*>(out + (size_t)((ib + par) & 1) * 32 * 16 + (size_t)ib * 16) = a;
       }
     }
   }
