@@ -227,9 +227,14 @@ __device__ __forceinline__ void update_planes(uint32_t* pl, int L, uint8_t* work
   const bool wolff = kind == MCRG_UPDATE_WOLFF;
   for (int x = tid; x < 2 * words; x += T) {
     const int c = x >= words, r = x - c * words, i = r >> (__ffs(wpr) - 1), w = r & (wpr - 1), q = (i + c) & 1;
+    // site p of the word has label word (i L + 64 w + 2 p + q) / 2, bank p: the lanes start at
+    // p = lane and go round, so that they read 32 different banks at every step
+    const int lane = tid & 31;
     uint32_t mask = 0;
-    for (int p = 0; p < 32; ++p)
+    for (int s = 0; s < 32; ++s) {
+      const int p = (s + lane) & 31;
       if (flips(work, L, i * L + 2 * (32 * w + p) + q, wolff)) mask |= 1u << planes::plane_pos(p);
+    }
     pl[x] ^= mask;
   }
   chain_sync(T);
