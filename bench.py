@@ -487,6 +487,11 @@ def served_cfg(args, D: Dist) -> dict:
             "p99_latency_s": top["p99_latency_s"], "rates": rates, "plain": plain,
             "served_over_plain_solves": round(top["solves_per_s"] / plain["solves_per_s"], 1),
             "loop": loop, "clocks": clocks,
+            "roofline": {"bound": "sm_issue", "kernel": "serve_kernel (its run_chain body on L = 1024 chains, the "
+                                                        "bulk of the stream's site updates)",
+                         "issue_active_frac": profiled("issue_active_frac", "pool_kernel_L1024_chains"),
+                         "source": "ncu, profiles/pool_kernel_L1024_chains.md (the same chain body in "
+                                   "pool_kernel<512,1>)"},
             "equal_error": "same seeds: served and plain runs give bit-identical moment sums (checked on the timed "
                            "plain requests)",
             "config": {"workload": "served: Poisson arrivals at 1e1, 1e2, 1e3, 1e4 /s (about 2 s of arrivals each, "
