@@ -187,8 +187,11 @@ __device__ void sweep_colour_vec(uint8_t* lat, int n, int c, uint32_t t, Key key
         load_words<NW>(Oc + (size_t)((i - 1) & (n - 1)) * half + k0, uw);
         load_words<NW>(Oc + (size_t)((i + 1) & (n - 1)) * half + k0, dw);
         load_words<NW>(orow + k0, mw);
-        const uint32_t prv = load_word(orow + ((k0 - 4) & (half - 1)));
-        const uint32_t nxt = load_word(orow + ((k0 + CB) & (half - 1)));
+        // the words before and after the chunk (wrapped in the row); a row of one chunk
+        // (L = 16, 32) has them in mw already (word loads at a 16-byte stride would put
+        // four lanes on each bank)
+        const uint32_t prv = cpr == 1 ? mw[NW - 1] : load_word(orow + ((k0 - 4) & (half - 1)));
+        const uint32_t nxt = cpr == 1 ? mw[0] : load_word(orow + ((k0 + CB) & (half - 1)));
         const uint4 R = stream_block(key, rep, P_SWEEP_HI, (uint32_t)c, (uint32_t)i, (uint32_t)(k0 >> 4), t);
         om[r] = update_chunk<NW>(tw, uw, dw, mw, prv, nxt, q, R, a);
         store_words<NW>(tp, tw);
