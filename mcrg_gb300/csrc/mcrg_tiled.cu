@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(256) level_kernel(const uint8_t* __restrict__ 
   __shared__ int part[8][5];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
   int a5[5] = {0, 0, 0, 0, 0};
-  couplings_vec<4>(in, n, tid, T, a5);
+  if (C <= 2) couplings_vec<4, 2>(in, n, tid, T, a5);  // two couplings read four rows instead of six
+  else couplings_vec<4>(in, n, tid, T, a5);
   if (do_block) block_vec(in, n, out, nullptr, key, rep, level_out, sample, tid, T);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -142,9 +143,15 @@ __global__ void __launch_bounds__(256) tail_kernel(TailJob J) {
     for (int l = lt; l <= nl; ++l, m >>= 1) {
       const uint8_t* lev = smem + plan.off[l - lt];
       int a5[5] = {0, 0, 0, 0, 0};
-      if (m >= 32) couplings_vec<4>(lev, m, tid, T, a5);
-      else if (m == 16) couplings_vec<2>(lev, m, tid, T, a5);
-      else couplings_scalar(lev, m, tid, T, a5);
+      if (m >= 32) {
+        if (C <= 2) couplings_vec<4, 2>(lev, m, tid, T, a5);
+        else couplings_vec<4>(lev, m, tid, T, a5);
+      } else if (m == 16) {
+        if (C <= 2) couplings_vec<2, 2>(lev, m, tid, T, a5);
+        else couplings_vec<2>(lev, m, tid, T, a5);
+      } else {
+        couplings_scalar(lev, m, tid, T, a5);
+      }
       reduce_into(a5, St + l * MCRG_MAX_COUPLINGS, C);
       if (l < nl) {
         uint8_t* nxt = smem + plan.off[l + 1 - lt];
