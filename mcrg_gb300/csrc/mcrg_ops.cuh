@@ -276,11 +276,13 @@ __device__ void sweep_colour_scalar(uint8_t* lat, int n, int c, uint32_t t, Key 
 // counts every bond from both ends).  Accumulates final values in acc[5].
 // ---------------------------------------------------------------------------
 // NC: number of couplings wanted (1..5); the sums past NC stay 0.
-template <int NW, int NC = 5>
+// U: tasks per thread and step (2 on HBM levels: twice the loads in flight).
+template <int NW, int NC = 5, int U = 1>
 __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&acc)[5]) {
   constexpr int CB = 4 * NW;
   const int half = n / 2, cpr = half / CB, lc = __ffs(cpr) - 1, lnc = __ffs(n * cpr) - 1;  // powers of two
-  for (int task = tid; task < 2 * n * cpr; task += T) {
+  const int ntask = 2 * n * cpr;
+  auto body = [&](int task) {
     const int c = task >> lnc, rem = task & (n * cpr - 1), i = rem >> lc, k0 = (rem & (cpr - 1)) * CB;
     const uint32_t q = (uint32_t)((i + c) & 1);
     const uint8_t* C = lev + (size_t)c * n * half;
@@ -325,7 +327,14 @@ __device__ void couplings_vec(const uint8_t* lev, int n, int tid, int T, int (&a
     if (NC > 2) acc[2] += 4 * CB - 4 * (int)bytesum(e);
     if (NC > 3) acc[3] += CB - 2 * (int)bytesum(p);
     if (NC > 4) acc[4] += 2 * CB - 2 * (int)bytesum(h);
-  }
+  };
+  int task = tid;
+  if (U > 1)
+    for (; task + T < ntask; task += 2 * T) {  // no stores: the two tasks' loads may all be issued first
+      body(task);
+      body(task + T);
+    }
+  for (; task < ntask; task += T) body(task);
 }
 
 __device__ __forceinline__ int spin_at(const uint8_t* lev, int n, int i, int j) {

@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(256) level_kernel(const uint8_t* __restrict__ 
   __shared__ int part[8][5];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
   int a5[5] = {0, 0, 0, 0, 0};
-  if (C <= 2) couplings_vec<4, 2>(in, n, tid, T, a5);  // two couplings read four rows instead of six
-  else couplings_vec<4>(in, n, tid, T, a5);
+  if (C <= 2) couplings_vec<4, 2, 2>(in, n, tid, T, a5);  // two couplings read four rows instead of six
+  else couplings_vec<4, 5, 2>(in, n, tid, T, a5);
   if (do_block) block_vec(in, n, out, nullptr, key, rep, level_out, sample, tid, T);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
