@@ -124,3 +124,16 @@ def test_cluster_chains_in_the_pool(M):
             assert_moments_equal(mom, tot)
         else:
             assert_moments_equal(mom, oracle_moments(r))
+
+
+@pytest.mark.parametrize("L", [64, 128, 256])
+def test_byte_chains_every_coupling_count(M, L):
+    """Outside the fast regime (K = -0.1) chains of side >= 64 keep their levels as bytes:
+    the levels of side >= 64 are measured by the whole chain, the level of side 32 is read
+    into one warp's row words from bytes; every coupling count gives the oracle's moments."""
+    reqs = [M.make_request(L, -0.1, seed=700 + L + C, replica=C, n_eq=2, n_samples=3, sweeps_between=1 + C % 2,
+                           n_couplings=C) for C in (1, 2, 3, 5)]
+    res = M.batch_run(reqs)
+    for r, (st, mom) in zip(reqs, res):
+        assert st == 0
+        assert_moments_equal(mom, oracle_moments(r))
